@@ -1,0 +1,18 @@
+#!/usr/bin/env bash
+# Builds the CPU oracle (test infrastructure): oracle/_build/liboracle32.so
+# (reference FP32 semantics) and liboracle64.so (FP64 continuous values).
+# -ffp-contract=off keeps every multiply and add separately rounded, as the
+# reference source is written (aarch64 gcc would otherwise fuse them).
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+OUT="$HERE/_build"
+mkdir -p "$OUT"
+CC="${CC:-gcc}"
+FLAGS=(-std=c11 -O2 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -Wall -Wno-unknown-pragmas -Wno-unused-but-set-variable)
+"$CC" "${FLAGS[@]}" -DFSR_REAL_BITS=32 -o "$OUT/liboracle32.so" "$HERE/fsr_oracle.c" -lm &
+P1=$!
+"$CC" "${FLAGS[@]}" -DFSR_REAL_BITS=64 -o "$OUT/liboracle64.so" "$HERE/fsr_oracle.c" -lm &
+P2=$!
+wait "$P1"
+wait "$P2"
+echo "build_oracle: wrote $OUT/liboracle32.so $OUT/liboracle64.so"
