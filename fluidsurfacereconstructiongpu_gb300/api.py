@@ -1,0 +1,292 @@
+"""Python front end over the C ABI (include/fsr.h).
+
+Two layers:
+
+* :class:`Reconstructor` - one handle, one frame per call, particles either
+  as CUDA tensors (device path, ``fsr_reconstruct``) or numpy arrays (host
+  path, ``fsr_reconstruct_host``);
+* the reference-named file-driven classes ``ReconstructorGPUOursZB05``,
+  ``ReconstructorGPUOursYu13``, ``ReconstructorGPUAkinci12`` (and a TC01
+  variant) with the public methods of ReconstructorGPU
+  (FluidSurfaceReconstruction/GPU/ReconstructorGPU.h:14-30).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+METHODS = {"zb05": N.METHOD_ZB05, "tc01": N.METHOD_TC01, "yu13": N.METHOD_YU13, "aniso": N.METHOD_YU13,
+           "akinci": N.METHOD_AKINCI12, "akinci12": N.METHOD_AKINCI12}
+
+
+def header_from(bbox_min, bbox_max, h, particle_radius, mass) -> N.FrameHeader:
+    hd = N.FrameHeader()
+    for a in range(3):
+        hd.bbox_min[a] = float(bbox_min[a])
+        hd.bbox_max[a] = float(bbox_max[a])
+    hd.kernel_radius = float(h)
+    hd.particle_radius = float(particle_radius)
+    hd.particle_mass = float(mass)
+    return hd
+
+
+def header_of(frame) -> N.FrameHeader:
+    """Header of a synthetic ParticleFrame (or anything with the same fields)."""
+    return header_from(frame.bbox_min, frame.bbox_max, frame.h, frame.particle_radius, frame.mass)
+
+
+def default_params(method: str) -> N.Params:
+    p = N.Params()
+    N.check(N.lib.fsr_default_params(METHODS[method], ctypes.byref(p)))
+    return p
+
+
+@dataclass
+class Mesh:
+    positions: np.ndarray  # (3T, 3) f32, triangle soup in the reference's order
+    normals: np.ndarray
+
+    @property
+    def n_triangles(self) -> int:
+        return self.positions.shape[0] // 3
+
+
+class Reconstructor:
+    """One reconstructor handle bound to a CUDA device."""
+
+    def __init__(self, method: str = "zb05", device: int = 0, *, iso: Optional[float] = None,
+                 grid_ratio: Optional[int] = None, cell_size_scale: Optional[float] = None,
+                 smoothing_lambda: Optional[float] = None, aniso_radius_over_h: Optional[float] = None,
+                 min_neighbors: Optional[int] = None, keep_intermediates: bool = False,
+                 stage_timing: bool = False):
+        self.method = method
+        p = default_params(method)
+        if iso is not None:
+            p.iso_value = iso
+        if grid_ratio is not None:
+            p.grid_ratio = grid_ratio
+        if cell_size_scale is not None:
+            p.cell_size_scale = cell_size_scale
+        if smoothing_lambda is not None:
+            p.smoothing_lambda = smoothing_lambda
+        if aniso_radius_over_h is not None:
+            p.aniso_radius_over_h = aniso_radius_over_h
+        if min_neighbors is not None:
+            p.min_neighbors = min_neighbors
+        p.flags = (N.FLAG_KEEP_INTERMEDIATES if keep_intermediates else 0) | \
+            (N.FLAG_STAGE_TIMING if stage_timing else 0)
+        self.params = p
+        h = ctypes.c_void_p()
+        st = N.lib.fsr_create(ctypes.byref(p), int(device), ctypes.byref(h))
+        if st != N.FSR_OK:
+            raise N.FsrError(st, "fsr_create failed")
+        self._h = h
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib.fsr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- frames
+    def reconstruct(self, xyz, density, header: N.FrameHeader, stream=None) -> int:
+        """Device path: xyz (N,3) and density (N,) float32 CUDA tensors.
+        Returns the number of mesh vertices; the mesh stays on the device."""
+        import torch
+        assert xyz.is_cuda and density.is_cuda, "device path needs CUDA tensors"
+        xyz = xyz.contiguous()
+        density = density.contiguous()
+        assert xyz.dtype == torch.float32 and density.dtype == torch.float32
+        n = int(density.numel())
+        s = stream if stream is not None else torch.cuda.current_stream(xyz.device)
+        st = N.lib.fsr_reconstruct(self._h, ctypes.byref(header), ctypes.c_void_p(xyz.data_ptr()),
+                                   ctypes.c_void_p(density.data_ptr()), n, ctypes.c_void_p(s.cuda_stream))
+        N.check(st, self._h)
+        return int(self.stats().n_mesh_vertices)
+
+    def reconstruct_host(self, xyz: np.ndarray, density: np.ndarray, header: N.FrameHeader,
+                         capacity: Optional[int] = None) -> Mesh:
+        """Host path: numpy in, numpy triangle soup out (copies included)."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        density = np.ascontiguousarray(density, dtype=np.float32).reshape(-1)
+        nv = ctypes.c_uint64(0)
+        cap = int(capacity) if capacity is not None else 0
+        pos = np.empty((max(cap, 1), 3), np.float32)
+        nrm = np.empty((max(cap, 1), 3), np.float32)
+        st = N.lib.fsr_reconstruct_host(self._h, ctypes.byref(header), xyz.ctypes.data, density.ctypes.data,
+                                        xyz.shape[0], pos.ctypes.data, nrm.ctypes.data, cap, ctypes.byref(nv),
+                                        None)
+        if st == 7:  # capacity: fetch with the right size
+            pos = np.empty((nv.value, 3), np.float32)
+            nrm = np.empty((nv.value, 3), np.float32)
+            N.check(N.lib.fsr_copy_mesh(self._h, pos.ctypes.data, nrm.ctypes.data, nv.value, ctypes.byref(nv)),
+                    self._h)
+            return Mesh(pos, nrm)
+        N.check(st, self._h)
+        return Mesh(pos[:nv.value], nrm[:nv.value])
+
+    def mesh(self) -> Mesh:
+        nv = int(self.stats().n_mesh_vertices)
+        pos = np.empty((max(nv, 1), 3), np.float32)
+        nrm = np.empty((max(nv, 1), 3), np.float32)
+        out = ctypes.c_uint64(0)
+        N.check(N.lib.fsr_copy_mesh(self._h, pos.ctypes.data, nrm.ctypes.data, nv, ctypes.byref(out)), self._h)
+        return Mesh(pos[:nv], nrm[:nv])
+
+    def mesh_device_ptrs(self):
+        p, q, nv = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
+        N.check(N.lib.fsr_mesh_device(self._h, ctypes.byref(p), ctypes.byref(q), ctypes.byref(nv)), self._h)
+        return p.value, q.value, nv.value
+
+    def stats(self) -> N.Stats:
+        s = N.Stats()
+        N.check(N.lib.fsr_get_stats(self._h, ctypes.byref(s)), self._h)
+        return s
+
+    def debug(self, name: str) -> np.ndarray:
+        which = N.DBG[name]
+        need = ctypes.c_uint64(0)
+        N.check(N.lib.fsr_debug_fetch(self._h, which, None, 0, ctypes.byref(need)), self._h)
+        dtype = np.float32 if name in ("sorted_xyz", "field", "mean", "smoothed", "G") else np.uint32
+        out = np.empty(need.value // 4, dtype=dtype)
+        if need.value:
+            N.check(N.lib.fsr_debug_fetch(self._h, which, out.ctypes.data, need.value, None), self._h)
+        if name in ("sorted_xyz", "mean", "smoothed"):
+            out = out.reshape(-1, 3)
+        elif name == "ranges":
+            out = out.reshape(-1, 2)
+        elif name == "G":
+            out = out.reshape(-1, 9)
+        return out
+
+
+def read_xyz(path: str):
+    """Parses an .xyz file; returns (header, xyz (N,3), density (N,))."""
+    hd = N.FrameHeader()
+    px, pd, n = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
+    N.check(N.lib.fsr_read_xyz(path.encode(), ctypes.byref(hd), ctypes.byref(px), ctypes.byref(pd),
+                               ctypes.byref(n)))
+    try:
+        cnt = n.value
+        xyz = np.ctypeslib.as_array((ctypes.c_float * (3 * max(cnt, 1))).from_address(px.value))[:3 * cnt]
+        den = np.ctypeslib.as_array((ctypes.c_float * max(cnt, 1)).from_address(pd.value))[:cnt]
+        xyz = xyz.reshape(-1, 3).copy()
+        den = den.copy()
+    finally:
+        N.lib.fsr_free_host(px)
+        N.lib.fsr_free_host(pd)
+    return hd, xyz, den
+
+
+def write_xyz(path: str, frame) -> None:
+    """Writes a ParticleFrame as .xyz (data_format.txt layout)."""
+    with open(path, "w") as f:
+        f.write("%.9g %.9g %.9g\n" % tuple(frame.bbox_min))
+        f.write("%.9g %.9g %.9g\n" % tuple(frame.bbox_max))
+        f.write("%.9g\n%.9g\n%.9g\n" % (frame.h, frame.particle_radius, frame.mass))
+        for p, d in zip(frame.pos, frame.density):
+            f.write("%.9g %.9g %.9g %.9g\n" % (p[0], p[1], p[2], d))
+
+
+def write_obj(path: str, mesh: Mesh) -> None:
+    pos = np.ascontiguousarray(mesh.positions, np.float32)
+    nrm = np.ascontiguousarray(mesh.normals, np.float32)
+    N.check(N.lib.fsr_write_obj(path.encode(), pos.ctypes.data, nrm.ctypes.data, pos.shape[0]))
+
+
+class ReconstructorGPU:
+    """File-driven reconstruction with the reference's public interface
+    (ReconstructorGPU.h:14-30): frames [from, to) of
+    directory + pattern % frame + '.xyz', meshes to the same stem + '.obj'."""
+
+    METHOD = "zb05"
+    ALGORITHM = ""
+
+    def __init__(self, directory: str, file_pattern: str, frame_from: int, frame_to: int, device: int = 0,
+                 **params):
+        self.directory = directory
+        self.file_pattern = file_pattern
+        self.frame_from, self.frame_to = int(frame_from), int(frame_to)
+        self._save_obj = True
+        self._save_cfg = False
+        self._rec = Reconstructor(self.METHOD, device, **params)
+        self._times: list[float] = []
+        self._num_particles = 0
+
+    def getAlgorithmType(self) -> str:
+        return self.ALGORITHM
+
+    def setOutputMeshFile(self, flag: bool):
+        self._save_obj = bool(flag)
+
+    def setOutputConfigFile(self, flag: bool):
+        self._save_cfg = bool(flag)
+
+    def setOutputVisualizeFile(self, flag: bool):
+        if flag:
+            raise NotImplementedError(".vis debug dumps are not produced by this library")
+
+    def getSimulationParameters(self) -> N.Params:
+        return self._rec.params
+
+    def getNumberOfParticles(self) -> int:
+        return int(self._rec.stats().n_particles) if self._times else 0
+
+    def getTimeConsumingSequence(self) -> list:
+        return list(self._times)
+
+    def reconstruct(self):
+        if self.frame_from >= self.frame_to:
+            raise ValueError("Wrong settings occur for frame range.")
+        n = self.frame_to - self.frame_from
+        ms = (ctypes.c_double * n)()
+        d = self.directory if self.directory.endswith(os.sep) or not self.directory else self.directory + os.sep
+        st = N.lib.fsr_reconstruct_files(self._rec._h, d.encode(), self.file_pattern.encode(),
+                                         self.frame_from, self.frame_to, 1 if self._save_obj else 0, ms)
+        N.check(st, self._rec._h)
+        self._times = list(ms)
+        if self._save_cfg:
+            s = self._rec.stats()
+            with open(os.path.join(d, self.ALGORITHM + ".config"), "w") as f:
+                f.write(f"{s.n_mesh_vertices // 3}\n{s.n_surface_particles / max(s.n_particles, 1)}\n"
+                        f"{s.n_band_vertices / max(s.n_grid_vertices, 1)}\n")
+        with open(os.path.join(d, self.ALGORITHM + ".time"), "a") as f:
+            f.write(" ".join("%g" % t for t in self._times) + " \n")
+
+
+class ReconstructorGPUOursZB05(ReconstructorGPU):
+    METHOD = "zb05"
+    ALGORITHM = "Our Algorithm using ZB05 kernel"
+
+
+class ReconstructorGPUOursTC01(ReconstructorGPU):
+    METHOD = "tc01"
+    ALGORITHM = "Our Algorithm using TC01 kernel"
+
+
+class ReconstructorGPUOursYu13(ReconstructorGPU):
+    METHOD = "yu13"
+    ALGORITHM = "Our Algorithm using anisotropic kernel"
+
+
+class ReconstructorGPUAkinci12(ReconstructorGPU):
+    METHOD = "akinci"
+    ALGORITHM = "Akinci12 using ZB05 kernel"

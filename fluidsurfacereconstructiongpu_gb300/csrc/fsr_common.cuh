@@ -1,0 +1,129 @@
+// Shared device-side definitions of the reconstruction kernels.
+//
+// Arithmetic policy.  Every value that feeds a discrete decision - a cell
+// index, a grid-vertex position, a band-membership or neighbour-count test,
+// a surface-particle test - is computed with explicitly rounded FP32
+// operations (__fadd_rn & co.) in the reference's operation order, so it
+// cannot be contracted into an FMA and the decision matches the reference
+// source evaluated in IEEE FP32 bit for bit.  Continuous accumulations that
+// only feed the field value (kernel sums, covariances) are free to use FMA
+// and any summation order; they are checked against the FP64 oracle within
+// the stated tolerance.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mc_tables.h"
+
+namespace fsr {
+
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+
+// Uniform grid (GridInfo, Defines.h:62-68, without the unused maxPos).
+struct Grid {
+    float min[3];
+    float cs;
+    uint32_t res[3];
+    uint32_t pad;
+};
+
+// Device-resident frame counters: sizes that later stages read, plus error
+// and capacity-overflow flags.  Filled by the kernels, read once per frame.
+struct Counters {
+    uint32_t n_band;         // B
+    uint32_t n_valid;        // Q
+    uint32_t n_mesh_verts;   // 3T
+    uint32_t n_surface;      // surface particles
+    uint32_t n_involved;     // Yu13 involved particles
+    uint32_t n_fp64;         // eigen solves redone in FP64
+    uint32_t out_of_grid;    // particles outside the grid (error)
+    uint32_t overflow;       // bit 0: band, bit 1: valid cubes, bit 2: mesh vertices
+    uint32_t need_band;      // sizes wanted when an overflow happened
+    uint32_t need_valid;
+    uint32_t need_mesh;
+    uint32_t pad[5];
+};
+
+// Rank directory over the band bitset: rank(v) = number of band vertices
+// with a smaller id, valid when v itself is in the band.
+struct BandView {
+    const uint32_t* bits;    // V bits
+    const uint32_t* prefix;  // exclusive prefix of popcount per 32-bit word
+    const float* phi;        // field per band vertex, in rank order
+};
+
+// Marching-cubes tables in constant memory.
+struct McConst {
+    uint64_t tri[256];
+    uint16_t eflags[256];
+    uint8_t nverts[256];
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint32_t lin3(uint32_t x, uint32_t y, uint32_t z, const Grid& g)
+{
+    return z * g.res[0] * g.res[1] + y * g.res[0] + x;
+}
+
+__device__ __forceinline__ void unlin3(uint32_t i, const Grid& g, uint32_t& x, uint32_t& y, uint32_t& z)
+{
+    const uint32_t xy = g.res[0] * g.res[1];
+    z = i / xy;
+    const uint32_t m = i - z * xy;
+    y = m / g.res[0];
+    x = m - y * g.res[0];
+}
+
+// getIndex3D (ReconstructionCUDA.cuh:354-358): trunc((p - min) / cs).
+__device__ __forceinline__ int cell1(float p, float mn, float cs)
+{
+    return __float2int_rz(__fdiv_rn(__fsub_rn(p, mn), cs));
+}
+
+// getVertexPos (ReconstructionCUDA.cuh:366-370): float(i) * cs + min, with
+// the product rounded before the sum.
+__device__ __forceinline__ float vpos1(uint32_t i, float mn, float cs)
+{
+    return __fadd_rn(__fmul_rn(__uint2float_rn(i), cs), mn);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// dot(d, d) of helper_math: (x*x + y*y) + z*z, each product rounded.
+__device__ __forceinline__ float dot3_rn(float x, float y, float z)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
+}
+
+// Cells c-ext .. c+ext clamped to the grid.
+struct Window {
+    int lo[3], hi[3];
+};
+
+__device__ __forceinline__ Window window(int cx, int cy, int cz, int ext, const Grid& g)
+{
+    Window w;
+    const int c[3] = {cx, cy, cz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        w.lo[a] = clampi(c[a] - ext, 0, (int)g.res[a] - 1);
+        w.hi[a] = clampi(c[a] + ext, 0, (int)g.res[a] - 1);
+    }
+    return w;
+}
+
+__device__ __forceinline__ bool band_has(const BandView& b, uint32_t v)
+{
+    return (__ldg(b.bits + (v >> 5)) >> (v & 31u)) & 1u;
+}
+
+__device__ __forceinline__ uint32_t band_rank(const BandView& b, uint32_t v)
+{
+    const uint32_t w = __ldg(b.bits + (v >> 5));
+    return __ldg(b.prefix + (v >> 5)) + __popc(w & ((1u << (v & 31u)) - 1u));
+}
+
+#endif  // __CUDACC__
+
+}  // namespace fsr

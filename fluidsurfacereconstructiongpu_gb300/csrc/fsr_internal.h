@@ -1,0 +1,71 @@
+// The reconstructor handle: parameters, pooled device buffers and the last
+// frame's bookkeeping.  Buffers only grow; they are released by
+// fsr_destroy.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fsr.h"
+#include "fsr_common.cuh"
+
+namespace fsr {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want);  // contents are not preserved on growth
+    void release();
+};
+
+bool derive_grids(const fsr_frame_header& hdr, const fsr_params& p, Grid& sp, Grid& sc, float* sp_max,
+                  uint64_t& C, uint64_t& V);
+float band_threshold(float h);
+uint32_t bits_for(uint64_t c);
+fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_xyz, const float* d_den,
+                     uint64_t n, cudaStream_t st);
+
+}  // namespace fsr
+
+struct fsr_handle {
+    fsr_params params{};
+    int device = 0;
+    int num_sms = 1;
+    std::string last_error;
+
+    // particle-sized
+    fsr::DevBuf in_xyz, in_den;          // staging for host input
+    fsr::DevBuf keys0, vals0, keys1, vals1, radix_tmp;
+    fsr::DevBuf sorted;                  // float4 x,y,z,density in cell order
+    fsr::DevBuf psurf;                   // Akinci12 per-particle surface flags
+    fsr::DevBuf mean, smoothed, grec;    // Yu13
+    fsr::DevBuf pflags;                  // u32 surface flags (debug)
+    // cell-sized
+    fsr::DevBuf ranges, occ, surf, invol;
+    // vertex-sized
+    fsr::DevBuf bits, prefix, scan_tmp;
+    // band-sized
+    fsr::DevBuf sv, phi, mc, vofs, qpos, valid;
+    // mesh
+    fsr::DevBuf mesh_pos, mesh_nrm;
+    fsr::DevBuf ctr;
+
+    uint32_t cap_band = 0, cap_valid = 0, cap_mesh = 0;
+    fsr::Counters* pinned_ctr = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev[FSR_NUM_STAGES] = {};
+
+    // last frame
+    bool frame_ready = false;
+    fsr_stats stats{};
+    fsr::Grid grid_sp{}, grid_sc{};
+    uint64_t n_last = 0, C_last = 0, V_last = 0;
+    const uint32_t* perm_ptr = nullptr;
+    const uint32_t* skeys_ptr = nullptr;
+
+    ~fsr_handle();
+    std::vector<fsr::DevBuf*> all_buffers();
+};

@@ -1,0 +1,862 @@
+// Per-frame kernels of the reconstruction path.  Each kernel names the
+// reference kernel it replaces (ReconstructionCUDA.cu, "cu").
+#include "kernels.h"
+
+#include <algorithm>
+
+namespace fsr {
+
+__constant__ McConst c_mc;
+
+void upload_mc_tables(cudaStream_t s)
+{
+    McConst h;
+    for (int i = 0; i < 256; ++i) {
+        h.tri[i] = mc::kTriPacked[i];
+        h.eflags[i] = mc::kDerived.eflags[i];
+        h.nverts[i] = mc::kDerived.nverts[i];
+    }
+    cudaMemcpyToSymbolAsync(c_mc, &h, sizeof(h), 0, cudaMemcpyHostToDevice, s);
+}
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(uint64_t n, int threads = kThreads)
+{
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + threads - 1) / threads, 0x7fffffffULL));
+}
+
+// grid for grid-stride kernels whose length is read on the device
+inline unsigned persistent_blocks(const KernelCtx& c, uint64_t cap, int per_sm = 8)
+{
+    const uint64_t want = (cap + kThreads - 1) / kThreads;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c.num_sms * per_sm));
+}
+
+__device__ __forceinline__ void warp_count(uint32_t* counter, bool pred)
+{
+    const uint32_t m = __ballot_sync(__activemask(), pred);
+    if (pred && (threadIdx.x & 31u) == (uint32_t)(__ffs(m) - 1)) atomicAdd(counter, __popc(m));
+}
+
+// ------------------------------------------------------------ hashing
+// calcParticlesHashKernel (cu:1379-1396) plus the bounds check the
+// reference lacks (cu:1391-1395 writes out of bounds for such particles).
+__global__ void k_hash(const float* __restrict__ xyz, uint32_t n, Grid sp, uint32_t* __restrict__ keys,
+                       uint32_t* __restrict__ vals, Counters* ctr)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float p[3] = {xyz[3ull * i], xyz[3ull * i + 1], xyz[3ull * i + 2]};
+    int c[3];
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float q = __fdiv_rn(__fsub_rn(p[a], sp.min[a]), sp.cs);
+        ok = ok && (q > -1.0f) && (q < (float)sp.res[a]);  // NaN fails too
+        c[a] = ok ? __float2int_rz(q) : 0;
+    }
+    keys[i] = ok ? lin3((uint32_t)c[0], (uint32_t)c[1], (uint32_t)c[2], sp) : 0u;
+    vals[i] = i;
+    if (!ok) atomicAdd(&ctr->out_of_grid, 1u);
+}
+
+// findCellRangeKernel (cu:1399-1435) fused with the gather of the sorted
+// particles (the reference sorts positions and densities in place,
+// cu:1461-1466) into one float4 per particle.
+__global__ void k_ranges_gather(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ perm,
+                                uint32_t n, const float* __restrict__ xyz, const float* __restrict__ dens,
+                                float4* __restrict__ sorted, uint2* __restrict__ ranges,
+                                uint8_t* __restrict__ occ)
+{
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t key = skeys[k];
+    const uint32_t prev = k > 0 ? skeys[k - 1] : kEmpty;
+    const uint32_t next = k + 1 < n ? skeys[k + 1] : kEmpty;
+    if (key != prev) {
+        ranges[key].x = k;
+        occ[key] = 1;
+    }
+    if (key != next) ranges[key].y = k + 1;
+    const uint32_t s = perm[k];
+    sorted[k] = make_float4(xyz[3ull * s], xyz[3ull * s + 1], xyz[3ull * s + 2], dens[s]);
+}
+
+// ------------------------------------------------------------ surface
+// extractionOfSurfaceParticles (cu:70-120): an occupied cell with an empty
+// cell in its clamped 3x3x3 neighbourhood is a surface cell; the last cell
+// layer of each axis is never tested (cu:81).
+__global__ void k_surface_cells(Grid sp, const uint8_t* __restrict__ occ, uint8_t* __restrict__ surf)
+{
+    const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C) return;
+    uint32_t x, y, z;
+    unlin3((uint32_t)t, sp, x, y, z);
+    uint8_t s = 0;
+    if (x < sp.res[0] - 1 && y < sp.res[1] - 1 && z < sp.res[2] - 1 && occ[t]) {
+        const Window w = window((int)x, (int)y, (int)z, 1, sp);
+        for (int zz = w.lo[2]; zz <= w.hi[2] && !s; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1] && !s; ++yy)
+                for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx)
+                    if (!occ[lin3(xx, yy, zz, sp)]) { s = 1; break; }
+    }
+    surf[t] = s;
+}
+
+// The involved cells of extractionOfSurfaceAndInvolveParticles (cu:519-550),
+// gathered instead of scattered: an occupied cell is involved when a surface
+// cell lies within +-2 cells on every axis.
+__global__ void k_involved_cells(Grid sp, const uint8_t* __restrict__ occ, const uint8_t* __restrict__ surf,
+                                 uint8_t* __restrict__ invol)
+{
+    const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= C) return;
+    uint8_t v = 0;
+    if (occ[t]) {
+        uint32_t x, y, z;
+        unlin3((uint32_t)t, sp, x, y, z);
+        const Window w = window((int)x, (int)y, (int)z, 2, sp);
+        for (int zz = w.lo[2]; zz <= w.hi[2] && !v; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1] && !v; ++yy)
+                for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx)
+                    if (surf[lin3(xx, yy, zz, sp)]) { v = 1; break; }
+    }
+    invol[t] = v;
+}
+
+// extractionOfSurfaceParticlesUsingColorField (cu:909-971, wSpikyGrad
+// cuh:324-334).  The decision |grad c| > 3 depends on a sum, so the sum is
+// taken in the reference's order with the reference's roundings (FP64 where
+// the source promotes).
+__global__ void k_colorfield(const float4* __restrict__ sorted, uint32_t n, const uint2* __restrict__ ranges,
+                             Grid sp, float h, double k_spiky, float mass, uint8_t* __restrict__ psurf)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4 p = sorted[t];
+    const Window w = window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
+                            cell1(p.z, sp.min[2], sp.cs), 1, sp);
+    uint32_t nn = 0;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy)
+            for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx) {
+                const uint2 r = ranges[lin3(xx, yy, zz, sp)];
+                if (r.x == kEmpty) continue;
+                for (uint32_t i = r.x; i < r.y; ++i) {
+                    const float4 q = sorted[i];
+                    float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
+                    const float d2 = dot3_rn(rx, ry, rz);
+                    if (!(d2 > 0.0f)) continue;
+                    ++nn;
+                    const float d = __fsqrt_rn(d2);
+                    float grad = 0.0f;
+                    if (!(d >= h)) {
+                        const float x = __double2float_rn(__dsub_rn(1.0, (double)__fdiv_rn(d, h)));
+                        grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, (double)x), (double)x));
+                    }
+                    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(d2));
+                    rx = __fmul_rn(rx, inv);
+                    ry = __fmul_rn(ry, inv);
+                    rz = __fmul_rn(rz, inv);
+                    const float coef = __fmul_rn(__fdiv_rn(mass, q.w), grad);
+                    sx = __fadd_rn(sx, __fmul_rn(coef, rx));
+                    sy = __fadd_rn(sy, __fmul_rn(coef, ry));
+                    sz = __fadd_rn(sz, __fmul_rn(coef, rz));
+                }
+            }
+    const bool s = nn < 25u || __fsqrt_rn(dot3_rn(sx, sy, sz)) > 3.0f;
+    psurf[t] = s ? 1 : 0;
+}
+
+// ------------------------------------------------------------ band
+// estimationOfSurfaceVertices (cu:554-595): vertices in the clamped box
+// idx-3 .. idx+3 (x upper bound exclusive) within 1.5h of a surface
+// particle.  `thr` is the largest float whose double value is below
+// 1.5*h, so dist <= thr reproduces the reference's double comparison.
+// Each (y,z) row of at most 6 vertices is OR-ed into the bitset with at most
+// two atomics.
+__global__ void k_band_stamp(const float4* __restrict__ sorted, const uint32_t* __restrict__ skeys,
+                             const uint8_t* __restrict__ surf, const uint8_t* __restrict__ psurf, uint32_t n,
+                             Grid sc, float thr, uint32_t* __restrict__ bits, Counters* ctr)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool is_s = false;
+    if (t < n) is_s = psurf ? psurf[t] != 0 : surf[skeys[t]] != 0;
+    warp_count(&ctr->n_surface, is_s);
+    if (!is_s) return;
+    const float4 p = sorted[t];
+    const Window w = window(cell1(p.x, sc.min[0], sc.cs), cell1(p.y, sc.min[1], sc.cs),
+                            cell1(p.z, sc.min[2], sc.cs), 3, sc);
+    if (w.hi[0] <= w.lo[0]) return;
+    for (int z = w.lo[2]; z <= w.hi[2]; ++z) {
+        const float dz = __fsub_rn(vpos1(z, sc.min[2], sc.cs), p.z);
+        for (int y = w.lo[1]; y <= w.hi[1]; ++y) {
+            const float dy = __fsub_rn(vpos1(y, sc.min[1], sc.cs), p.y);
+            const uint32_t v0 = lin3(w.lo[0], y, z, sc);
+            const uint32_t word0 = v0 >> 5;
+            uint32_t m0 = 0, m1 = 0;
+            for (int x = w.lo[0]; x < w.hi[0]; ++x) {
+                const float dx = __fsub_rn(vpos1(x, sc.min[0], sc.cs), p.x);
+                const float dist = __fsqrt_rn(dot3_rn(dx, dy, dz));
+                if (dist <= thr) {
+                    const uint32_t v = v0 + (uint32_t)(x - w.lo[0]);
+                    if ((v >> 5) == word0) m0 |= 1u << (v & 31u);
+                    else m1 |= 1u << (v & 31u);
+                }
+            }
+            if (m0) atomicOr(bits + word0, m0);
+            if (m1) atomicOr(bits + word0 + 1, m1);
+        }
+    }
+}
+
+// compactSurfaceVertex (cu:293-304) over the bitset: every set bit writes
+// its vertex id at its rank.
+__global__ void k_band_list(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ prefix,
+                            uint32_t nwords, uint32_t* __restrict__ sv, uint32_t cap, Counters* ctr)
+{
+    const uint32_t nb = ctr->n_band;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && nb > cap) {
+        atomicOr(&ctr->overflow, 1u);
+        atomicMax(&ctr->need_band, nb);
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += gridDim.x * blockDim.x) {
+        uint32_t w = bits[i];
+        uint32_t r = prefix[i];
+        while (w) {
+            const uint32_t b = __ffs(w) - 1;
+            w &= w - 1;
+            if (r < cap) sv[r] = (i << 5) | b;
+            ++r;
+        }
+    }
+}
+
+// ------------------------------------------------------------ isotropic fields
+// updateScalarFieldValueZB05 (cu:230-289) and updateScalarFieldValueTC01
+// (cu:178-227): +-1 cell window around the vertex's cell.  A ZB05 vertex
+// with no weight keeps 0, the reference's memset value (cu:284).
+template <Field F>
+__global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Counters* ctr)
+{
+    const uint32_t nb = min(ctr->n_band, a.cap);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
+        uint32_t x, y, z;
+        unlin3(a.sv[t], a.sc, x, y, z);
+        const float vx = vpos1(x, a.sc.min[0], a.sc.cs), vy = vpos1(y, a.sc.min[1], a.sc.cs),
+                    vz = vpos1(z, a.sc.min[2], a.sc.cs);
+        const Window w = window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
+                                cell1(vz, a.sp.min[2], a.sp.cs), 1, a.sp);
+        float ws = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                // cells xx = lo..hi of this row are contiguous in the sorted array
+                const uint32_t c0 = lin3(w.lo[0], yy, zz, a.sp);
+                uint32_t beg = kEmpty, end = 0;
+                for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                    const uint2 r = __ldg(&a.ranges[c0 + xx]);
+                    if (r.x != kEmpty) {
+                        beg = min(beg, r.x);
+                        end = max(end, r.y);
+                    }
+                }
+                for (uint32_t i = beg; i < end; ++i) {
+                    const float4 q = __ldg(&a.sorted[i]);
+                    const float dx = vx - q.x, dy = vy - q.y, dz = vz - q.z;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (F == Field::kZB05) {
+                        if (d2 < a.h2) {
+                            const float u = 1.0f - d2 * a.inv_h2;
+                            const float wt = u * u * u;
+                            ws += wt;
+                            ax = fmaf(q.x, wt, ax);
+                            ay = fmaf(q.y, wt, ay);
+                            az = fmaf(q.z, wt, az);
+                        }
+                    } else {
+                        if (d2 <= a.h2) {
+                            const float u = d2 * a.inv_h2 * 0.5f;
+                            ws += u * u - u + 0.25f;
+                        }
+                    }
+                }
+            }
+        float phi;
+        if (F == Field::kZB05) {
+            if (ws > 0.f) {
+                const float inv = 1.0f / ws;
+                const float ex = vx - ax * inv, ey = vy - ay * inv, ez = vz - az * inv;
+                phi = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - a.rp;
+            } else {
+                phi = 0.f;
+            }
+        } else {
+            phi = ws;
+        }
+        a.phi[t] = phi;
+    }
+}
+
+// ------------------------------------------------------------ anisotropic path
+// calculationOfMeanAndSmoothParticles (cu:598-658).  The mean decides the
+// neighbour counts of the covariance stage, so it is summed in the
+// reference's order with the reference's roundings.  smoothed.w = m / rho.
+__global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
+                                                     const uint2* __restrict__ ranges, Grid sp, float R,
+                                                     float one_minus_lambda, float lambda, float mass,
+                                                     float4* __restrict__ mean, float4* __restrict__ smoothed)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4 p = sorted[t];
+    const Window w = window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
+                            cell1(p.z, sp.min[2], sp.cs), 2, sp);
+    float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+            const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
+            uint32_t beg = kEmpty, end = 0;
+            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                const uint2 r = __ldg(&ranges[c0 + xx]);
+                if (r.x != kEmpty) {
+                    beg = min(beg, r.x);
+                    end = max(end, r.y);
+                }
+            }
+            for (uint32_t i = beg; i < end; ++i) {
+                const float4 q = __ldg(&sorted[i]);
+                const float d = __fsqrt_rn(dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z)));
+                float wt = 0.f;
+                if (d < R) {
+                    const float s = __fdiv_rn(d, R);
+                    wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
+                }
+                ws = __fadd_rn(ws, wt);
+                mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
+                my = __fadd_rn(my, __fmul_rn(q.y, wt));
+                mz = __fadd_rn(mz, __fmul_rn(q.z, wt));
+            }
+        }
+    // ws >= 1: the particle itself has weight 1
+    mx = __fdiv_rn(mx, ws);
+    my = __fdiv_rn(my, ws);
+    mz = __fdiv_rn(mz, ws);
+    mean[t] = make_float4(mx, my, mz, 0.f);
+    smoothed[t] = make_float4(__fadd_rn(__fmul_rn(one_minus_lambda, p.x), __fmul_rn(lambda, mx)),
+                              __fadd_rn(__fmul_rn(one_minus_lambda, p.y), __fmul_rn(lambda, my)),
+                              __fadd_rn(__fmul_rn(one_minus_lambda, p.z), __fmul_rn(lambda, mz)),
+                              __fdiv_rn(mass, p.w));
+}
+
+// Kahan-compensated FP32 accumulator.
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
+// Loan, Matrix Computations, sec. 8.5); columns of V are eigenvectors.
+template <class T>
+__device__ void sym_eig3(T A[3][3], T wv[3], T V[3][3])
+{
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? T(1) : T(0);
+    const T tol = sizeof(T) == 4 ? T(1e-14) : T(1e-30);
+    for (int sweep = 0; sweep < (sizeof(T) == 4 ? 12 : 24); ++sweep) {
+        const T off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        const T dia = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+        if (!(off > tol * dia)) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0;
+            const int q = pq == 0 ? 1 : 2;
+            const T apq = A[p][q];
+            if (apq == T(0)) continue;
+            const T theta = (A[q][q] - A[p][p]) / (T(2) * apq);
+            const T sgn = theta >= T(0) ? T(1) : T(-1);
+            const T tt = sgn / (fabs(theta) + sqrt(theta * theta + T(1)));
+            const T cs = T(1) / sqrt(tt * tt + T(1));
+            const T sn = tt * cs;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T akp = A[k][p], akq = A[k][q];
+                A[k][p] = cs * akp - sn * akq;
+                A[k][q] = sn * akp + cs * akq;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T apk = A[p][k], aqk = A[q][k];
+                A[p][k] = cs * apk - sn * aqk;
+                A[q][k] = sn * apk + cs * aqk;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const T vkp = V[k][p], vkq = V[k][q];
+                V[k][p] = cs * vkp - sn * vkq;
+                V[k][q] = sn * vkp + cs * vkq;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) wv[i] = A[i][i];
+}
+
+// G = (1/h) cbrt(s1 s2 s3) V diag(1/s) V^T with s = |eigenvalues| clamped
+// from below at max(s)/4 (cu:790-822).  Returns the largest support radius
+// |r| with |G r| < 1, i.e. smax / cof.
+template <class T>
+__device__ float make_G(const T V[3][3], const T w[3], float h_inv, float G[9])
+{
+    T s0 = fabs(w[0]), s1 = fabs(w[1]), s2 = fabs(w[2]);
+    const T smax = fmax(s0, fmax(s1, s2));
+    const T lo = smax / T(4);
+    s0 = fmax(s0, lo);
+    s1 = fmax(s1, lo);
+    s2 = fmax(s2, lo);
+    const T cof = T(h_inv) * cbrt(s0 * s1 * s2);
+    const T inv[3] = {T(1) / s0, T(1) / s1, T(1) / s2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            T acc = T(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc += V[i][k] * inv[k] * V[j][k];
+            G[3 * i + j] = (float)(acc * cof);
+        }
+    return (float)(smax / cof);
+}
+
+// calculationOfTransformMatricesForParticles (cu:689-827) for every
+// particle of an involved cell.  The neighbour count (dist <= r about the
+// FP32 mean, cu:746) is exact; the covariance is accumulated with Kahan
+// compensation; the eigen-decomposition runs in FP32 and is redone in FP64
+// when the covariance's condition number exceeds 1e4.
+// Output record per particle: (x,y,z smoothed, r2max) (G row 0, coef)
+// (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
+__global__ void __launch_bounds__(kThreads) k_cov(CovArgs a, Counters* ctr)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool act = t < a.n && a.invol[a.skeys[t]];
+    warp_count(&ctr->n_involved, act);
+    if (!act) return;
+    const float4 p = a.sorted[t];
+    const float4 m = a.mean[t];
+    const Window w = window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
+                            cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp);
+    Kahan c11, c22, c33, c12, c13, c23, wsum;
+    uint32_t nn = 0;
+    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+            const uint32_t c0 = lin3(w.lo[0], yy, zz, a.sp);
+            uint32_t beg = kEmpty, end = 0;
+            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                const uint2 r = __ldg(&a.ranges[c0 + xx]);
+                if (r.x != kEmpty) {
+                    beg = min(beg, r.x);
+                    end = max(end, r.y);
+                }
+            }
+            for (uint32_t i = beg; i < end; ++i) {
+                const float4 q = __ldg(&a.sorted[i]);
+                const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
+                const float d = __fsqrt_rn(dot3_rn(vx, vy, vz));
+                if (d <= a.R) ++nn;
+                if (d < a.R) {
+                    const float s = d / a.R;
+                    const float wt = 1.0f - s * s * s;
+                    wsum.add(wt);
+                    const float wx = wt * vx, wy = wt * vy;
+                    c11.add(wx * vx);
+                    c22.add(wy * vy);
+                    c33.add(wt * vz * vz);
+                    c12.add(wx * vy);
+                    c13.add(wx * vz);
+                    c23.add(wy * vz);
+                }
+            }
+        }
+    float G[9];
+    float rmax;
+    if (nn < a.min_neighbors) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G[k] = 0.f;
+        G[0] = G[4] = G[8] = a.h_inv;
+        rmax = a.h;
+    } else {
+        const float iw = 1.0f / wsum.s;
+        // (h^2 I + sum) / wsum, the reference's seeded covariance (cu:718-723)
+        float A[3][3] = {{(a.h2 + c11.s) * iw, c12.s * iw, c13.s * iw},
+                         {c12.s * iw, (a.h2 + c22.s) * iw, c23.s * iw},
+                         {c13.s * iw, c23.s * iw, (a.h2 + c33.s) * iw}};
+        const float A0[3][3] = {{A[0][0], A[0][1], A[0][2]}, {A[1][0], A[1][1], A[1][2]}, {A[2][0], A[2][1], A[2][2]}};
+        float wv[3], V[3][3];
+        sym_eig3<float>(A, wv, V);
+        const float smax = fmaxf(fabsf(wv[0]), fmaxf(fabsf(wv[1]), fabsf(wv[2])));
+        const float smin = fminf(fabsf(wv[0]), fminf(fabsf(wv[1]), fabsf(wv[2])));
+        if (!(smin > 0.f) || smax > 1e4f * smin) {
+            double Ad[3][3], wd[3], Vd[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) Ad[i][j] = (double)A0[i][j];
+            sym_eig3<double>(Ad, wd, Vd);
+            rmax = make_G<double>(Vd, wd, a.h_inv, G);
+            atomicAdd(&ctr->n_fp64, 1u);
+        } else {
+            rmax = make_G<float>(V, wv, a.h_inv, G);
+        }
+    }
+    const float det = G[0] * G[4] * G[8] + G[1] * G[5] * G[6] + G[2] * G[3] * G[7] - G[0] * G[5] * G[7] -
+                      G[1] * G[3] * G[8] - G[2] * G[4] * G[6];
+    const float4 sm = a.smoothed[t];
+    const float r2 = rmax * rmax * 1.0001f;
+    float4* rec = a.grec + 4ull * t;
+    rec[0] = make_float4(sm.x, sm.y, sm.z, r2);
+    rec[1] = make_float4(G[0], G[1], G[2], a.sigma * det * sm.w);
+    rec[2] = make_float4(G[3], G[4], G[5], 0.f);
+    rec[3] = make_float4(G[6], G[7], G[8], 0.f);
+}
+
+// computationOfScalarFieldGrid (cu:830-906): +-2 cell window; particles of
+// involved cells use sigma det(G) (1 - |G r|^2)^3, all other particles the
+// unscaled sigma (1 - |r|^2)^3 (cuh:312-322), each times m / rho.
+__global__ void __launch_bounds__(kThreads) k_field_aniso(AnisoFieldArgs a, const Counters* ctr)
+{
+    const uint32_t nb = min(ctr->n_band, a.cap);
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
+        uint32_t x, y, z;
+        unlin3(a.sv[t], a.sc, x, y, z);
+        const float vx = vpos1(x, a.sc.min[0], a.sc.cs), vy = vpos1(y, a.sc.min[1], a.sc.cs),
+                    vz = vpos1(z, a.sc.min[2], a.sc.cs);
+        const Window w = window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
+                                cell1(vz, a.sp.min[2], a.sp.cs), 2, a.sp);
+        float sum = 0.f;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy)
+                for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx) {
+                    const uint32_t c = lin3(xx, yy, zz, a.sp);
+                    const uint2 r = __ldg(&a.ranges[c]);
+                    if (r.x == kEmpty) continue;
+                    if (__ldg(&a.invol[c])) {
+                        for (uint32_t i = r.x; i < r.y; ++i) {
+                            const float4 r0 = __ldg(&a.grec[4ull * i]);
+                            const float rx = r0.x - vx, ry = r0.y - vy, rz = r0.z - vz;
+                            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                            if (d2 >= r0.w) continue;
+                            const float4 g0 = __ldg(&a.grec[4ull * i + 1]);
+                            const float4 g1 = __ldg(&a.grec[4ull * i + 2]);
+                            const float4 g2 = __ldg(&a.grec[4ull * i + 3]);
+                            const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
+                            const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
+                            const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
+                            const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+                            if (q2 < 1.0f) {
+                                const float u = 1.0f - q2;
+                                sum = fmaf(g0.w, u * u * u, sum);
+                            }
+                        }
+                    } else {
+                        for (uint32_t i = r.x; i < r.y; ++i) {
+                            const float4 s = __ldg(&a.smoothed[i]);
+                            const float rx = s.x - vx, ry = s.y - vy, rz = s.z - vz;
+                            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                            if (d2 < 1.0f) {
+                                const float u = 1.0f - d2;
+                                sum = fmaf(a.sigma * s.w, u * u * u, sum);
+                            }
+                        }
+                    }
+                }
+        a.phi[t] = sum - 0.5f;
+    }
+}
+
+// ------------------------------------------------------------ marching cubes
+__device__ __forceinline__ float field_at(const McArgs& a, int x, int y, int z)
+{
+    if (x < 0 || y < 0 || z < 0 || (uint32_t)x >= a.sc.res[0] || (uint32_t)y >= a.sc.res[1] ||
+        (uint32_t)z >= a.sc.res[2])
+        return 0.f;  // getValue outside the grid (cuh:410-416)
+    const uint32_t v = lin3(x, y, z, a.sc);
+    if (!band_has(a.band, v)) return a.fill;
+    const uint32_t r = band_rank(a.band, v);
+    return r < a.cap_band ? __ldg(a.band.phi + r) : a.fill;  // r >= cap only in a frame that is re-run
+}
+
+// detectValidSurfaceCubes (cu:328-364): a band vertex as cube origin is
+// valid when all 8 corners are band vertices and the case emits triangles.
+__global__ void __launch_bounds__(kThreads) k_mc_classify(McArgs a, const Counters* ctr)
+{
+    const uint32_t nb = min(ctr->n_band, a.cap_band);
+    const uint32_t rx = a.sc.res[0], rxy = a.sc.res[0] * a.sc.res[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
+        const uint32_t v = a.sv[t];
+        uint32_t x, y, z;
+        unlin3(v, a.sc, x, y, z);
+        uint32_t info = 0;
+        if (x < a.sc.res[0] - 1 && y < a.sc.res[1] - 1 && z < a.sc.res[2] - 1) {
+            bool all = true;
+            uint32_t ids[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                ids[i] = v + (uint32_t)mc::cornerDx(i) + (uint32_t)mc::cornerDy(i) * rx +
+                         (uint32_t)mc::cornerDz(i) * rxy;
+                all = all && band_has(a.band, ids[i]);
+            }
+            if (all) {
+                uint32_t cs = 0;
+#pragma unroll
+                bool in_cap = true;
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t r = i == 0 ? t : (i == 4 ? t + 1 : band_rank(a.band, ids[i]));
+                    // ranks beyond the capacity only occur in a frame that overflowed and is re-run
+                    if (r >= a.cap_band) {
+                        in_cap = false;
+                        break;
+                    }
+                    if (__ldg(a.band.phi + r) <= a.iso) cs |= 1u << i;
+                }
+                if (in_cap) info = (uint32_t)c_mc.nverts[cs] | (cs << 8);
+            }
+        }
+        a.mc[t] = info;
+    }
+}
+
+__global__ void k_valid_list(McArgs a, Counters* ctr)
+{
+    const uint32_t nb = min(ctr->n_band, a.cap_band);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (ctr->n_valid > a.cap_valid) {
+            atomicOr(&ctr->overflow, 2u);
+            atomicMax(&ctr->need_valid, ctr->n_valid);
+        }
+        if (ctr->n_mesh_verts > a.cap_mesh) {
+            atomicOr(&ctr->overflow, 4u);
+            atomicMax(&ctr->need_mesh, ctr->n_mesh_verts);
+        }
+    }
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
+        if ((a.mc[t] & 0xFFu) != 0u) {
+            const uint32_t q = a.qpos[t];
+            if (q < a.cap_valid) a.valid[q] = t;
+        }
+    }
+}
+
+__device__ __forceinline__ void normalize_fast(float n[3])
+{
+    const float inv = rsqrtf(fmaf(n[0], n[0], fmaf(n[1], n[1], n[2] * n[2])));
+    n[0] *= inv;
+    n[1] *= inv;
+    n[2] *= inv;
+}
+
+// fVector3::normalize (MathVector.cpp:5-15): scaled only when longer than 1e-7
+__device__ __forceinline__ void normalize_guarded(float n[3])
+{
+    const float len = sqrtf(fmaf(n[0], n[0], fmaf(n[1], n[1], n[2] * n[2])));
+    if (len > 1.0e-7f) {
+        const float f = 1.0f / len;
+        n[0] *= f;
+        n[1] *= f;
+        n[2] *= f;
+    }
+}
+
+// generateTriangles (cu:383-463), or with host_mc the host marching cubes
+// of Akinci12 (MarchingCubesCPU.cpp:3-72: no normal sign flip, guarded
+// normalisation, epsilon test in double).
+__global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counters* ctr)
+{
+    const uint32_t nq = min(ctr->n_valid, a.cap_valid);
+    const uint32_t ntot = ctr->n_mesh_verts;
+    if (ntot > a.cap_mesh) return;
+    const float sgn = a.host_mc ? 1.0f : (a.iso < 0.0f ? -1.0f : 1.0f);
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const uint32_t t = a.valid[q];
+        const uint32_t info = a.mc[t];
+        const uint32_t cs = info >> 8;
+        const uint32_t nv = info & 0xFFu;
+        const uint32_t base = a.vofs[t];
+        uint32_t x, y, z;
+        unlin3(a.sv[t], a.sc, x, y, z);
+        float val[8], cp[8][3], cn[8][3];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int cx = (int)x + mc::cornerDx(i), cy = (int)y + mc::cornerDy(i),
+                      cz = (int)z + mc::cornerDz(i);
+            val[i] = field_at(a, cx, cy, cz);
+            cp[i][0] = vpos1(cx, a.sc.min[0], a.sc.cs);
+            cp[i][1] = vpos1(cy, a.sc.min[1], a.sc.cs);
+            cp[i][2] = vpos1(cz, a.sc.min[2], a.sc.cs);
+            cn[i][0] = field_at(a, cx - 1, cy, cz) - field_at(a, cx + 1, cy, cz);
+            cn[i][1] = field_at(a, cx, cy - 1, cz) - field_at(a, cx, cy + 1, cz);
+            cn[i][2] = field_at(a, cx, cy, cz - 1) - field_at(a, cx, cy, cz + 1);
+            if (a.host_mc) normalize_guarded(cn[i]);
+            else normalize_fast(cn[i]);
+        }
+        const uint32_t ef = c_mc.eflags[cs];
+        float ip[12][3], in[12][3];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) {
+            if (!(ef & (1u << e))) continue;
+            const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
+            const float d = val[i1] - val[i0];
+            const float f = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - val[i0]) / d;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                ip[e][k] = fmaf(f, cp[i1][k] - cp[i0][k], cp[i0][k]);
+                in[e][k] = fmaf(f, cn[i1][k] - cn[i0][k], cn[i0][k]);
+            }
+            if (a.host_mc) normalize_guarded(in[e]);
+            else normalize_fast(in[e]);
+        }
+        const uint64_t tri = c_mc.tri[cs];
+        for (uint32_t k = 0; k < nv; ++k) {
+            const int e = (int)((tri >> (4u * k)) & 0xFu);
+            const uint64_t o = 3ull * (base + k);
+            float px = 0.f, py = 0.f, pz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+#pragma unroll
+            for (int ee = 0; ee < 12; ++ee)
+                if (ee == e) {
+                    px = ip[ee][0]; py = ip[ee][1]; pz = ip[ee][2];
+                    nx = in[ee][0]; ny = in[ee][1]; nz = in[ee][2];
+                }
+            a.out_pos[o] = px;
+            a.out_pos[o + 1] = py;
+            a.out_pos[o + 2] = pz;
+            a.out_nrm[o] = sgn * nx;
+            a.out_nrm[o + 1] = sgn * ny;
+            a.out_nrm[o + 2] = sgn * nz;
+        }
+    }
+}
+
+__global__ void k_particle_flags(const uint32_t* __restrict__ skeys, const uint8_t* __restrict__ surf,
+                                 const uint8_t* __restrict__ psurf, uint32_t n, uint32_t* __restrict__ out)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    out[t] = psurf ? psurf[t] : surf[skeys[t]];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ launchers
+
+void launch_hash(const KernelCtx& c, const float* xyz, uint32_t n, const Grid& sp, uint32_t* keys,
+                 uint32_t* vals, Counters* ctr)
+{
+    if (!n) return;
+    k_hash<<<blocks_for(n), kThreads, 0, c.stream>>>(xyz, n, sp, keys, vals, ctr);
+}
+
+void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint32_t* perm, uint32_t n,
+                          const float* xyz, const float* dens, float4* sorted, uint2* ranges, uint8_t* occ)
+{
+    if (!n) return;
+    k_ranges_gather<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, perm, n, xyz, dens, sorted, ranges, occ);
+}
+
+void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf)
+{
+    const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
+    k_surface_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf);
+}
+
+void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, const uint8_t* surf,
+                           uint8_t* invol)
+{
+    const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
+    k_involved_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf, invol);
+}
+
+void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges,
+                       const Grid& sp, float h, float h2, float mass, uint8_t* psurf)
+{
+    if (!n) return;
+    // -45 / (pi h^4) exactly as the reference evaluates it in double
+    const double k = -45.0 / (3.1415926535 * (double)h2 * (double)h2);
+    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, h, k, mass, psurf);
+}
+
+void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t* skeys, const uint8_t* surf,
+                       const uint8_t* psurf, uint32_t n, const Grid& sc, float thr, uint32_t* bits,
+                       Counters* ctr)
+{
+    if (!n) return;
+    k_band_stamp<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc, thr, bits, ctr);
+}
+
+void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
+                      uint32_t* sv, uint32_t cap, Counters* ctr)
+{
+    k_band_list<<<persistent_blocks(c, nwords, 16), kThreads, 0, c.stream>>>(bits, prefix, nwords, sv, cap, ctr);
+}
+
+void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr)
+{
+    const unsigned g = persistent_blocks(c, a.cap, 16);
+    if (f == Field::kTC01) k_field_iso<Field::kTC01><<<g, kThreads, 0, c.stream>>>(a, ctr);
+    else k_field_iso<Field::kZB05><<<g, kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
+                   float R, float lambda, float mass, float4* mean, float4* smoothed)
+{
+    if (!n) return;
+    // (1.0 - lambda) is evaluated in double and rounded (cu:656)
+    const float oml = (float)(1.0 - (double)lambda);
+    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, oml, lambda, mass, mean, smoothed);
+}
+
+void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr)
+{
+    if (!a.n) return;
+    k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr)
+{
+    k_field_aniso<<<persistent_blocks(c, a.cap, 16), kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr)
+{
+    k_mc_classify<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_valid_list(const KernelCtx& c, const McArgs& a, Counters* ctr)
+{
+    k_valid_list<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr)
+{
+    k_mc_generate<<<persistent_blocks(c, a.cap_valid, 16), kThreads, 0, c.stream>>>(a, ctr);
+}
+
+void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint8_t* surf, const uint8_t* psurf,
+                           uint32_t n, uint32_t* out)
+{
+    if (!n) return;
+    k_particle_flags<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, surf, psurf, n, out);
+}
+
+}  // namespace fsr

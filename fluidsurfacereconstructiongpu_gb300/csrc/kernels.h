@@ -1,0 +1,114 @@
+// Launch wrappers of the per-frame kernels.  All are asynchronous on the
+// given stream; sizes that are only known on the device (band vertices,
+// valid cubes, mesh vertices) are read from Counters inside the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fsr_common.cuh"
+
+namespace fsr {
+
+enum class Field : int { kZB05 = 0, kTC01 = 1, kAniso = 2 };
+
+struct KernelCtx {
+    cudaStream_t stream;
+    int num_sms;
+};
+
+// spatial hashing: keys[i] = cell id, vals[i] = i.
+void launch_hash(const KernelCtx& c, const float* xyz, uint32_t n, const Grid& sp, uint32_t* keys,
+                 uint32_t* vals, Counters* ctr);
+
+// cell ranges, occupancy, sorted float4 (x,y,z,density) gather.
+void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint32_t* perm, uint32_t n,
+                          const float* xyz, const float* dens, float4* sorted, uint2* ranges,
+                          uint8_t* occ);
+
+void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf);
+void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, const uint8_t* surf,
+                           uint8_t* invol);
+
+// Akinci12 colour-field surface flags per sorted particle (u8).
+void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges,
+                       const Grid& sp, float h, float h2, float mass, uint8_t* psurf);
+
+// Band stamp around surface particles.  Surface particles are those with
+// psurf[i] != 0 when psurf is given, else those whose cell has surf != 0.
+void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t* skeys,
+                       const uint8_t* surf, const uint8_t* psurf, uint32_t n, const Grid& sc,
+                       float thr, uint32_t* bits, Counters* ctr);
+
+void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
+                      uint32_t* sv, uint32_t cap, Counters* ctr);
+
+struct IsoFieldArgs {
+    Grid sp, sc;
+    const float4* sorted;
+    const uint2* ranges;
+    const uint32_t* sv;
+    float* phi;
+    float h2, inv_h2, rp;
+    uint32_t cap;
+};
+void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr);
+
+// Yu13 smoothing: mean (exact FP32) and smoothed position with m/rho in w.
+void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
+                   float R, float lambda, float mass, float4* mean, float4* smoothed);
+
+struct CovArgs {
+    Grid sp;
+    const float4* sorted;
+    const float4* mean;
+    const float4* smoothed;  // x,y,z smoothed, w = m / rho
+    const uint2* ranges;
+    const uint32_t* skeys;
+    const uint8_t* invol;
+    float4* grec;  // 3 float4 per particle: G row-major, coef, r2max
+    uint32_t n;
+    float R, h, h2, h_inv, mass, sigma;
+    uint32_t min_neighbors;
+};
+void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr);
+
+struct AnisoFieldArgs {
+    Grid sp, sc;
+    const float4* smoothed;
+    const float4* grec;
+    const uint2* ranges;
+    const uint8_t* invol;
+    const uint8_t* occ;
+    const uint32_t* sv;
+    float* phi;
+    float sigma;
+    uint32_t cap;
+};
+void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr);
+
+struct McArgs {
+    Grid sc;
+    BandView band;
+    const uint32_t* sv;
+    uint32_t* mc;          // per band vertex: nverts | case << 8
+    const uint32_t* vofs;  // exclusive scan of nverts
+    const uint32_t* qpos;  // exclusive scan of (nverts != 0)
+    uint32_t* valid;       // valid cube list (positions in sv)
+    float* out_pos;
+    float* out_nrm;
+    float iso, fill;
+    int host_mc;           // Akinci12: the host marching cubes' normal/lerp rules
+    uint32_t cap_band, cap_valid, cap_mesh;
+};
+void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr);
+void launch_valid_list(const KernelCtx& c, const McArgs& a, Counters* ctr);
+void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr);
+
+// per-sorted-particle u32 surface flags (parity output)
+void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint8_t* surf,
+                           const uint8_t* psurf, uint32_t n, uint32_t* out);
+
+void upload_mc_tables(cudaStream_t s);
+
+}  // namespace fsr

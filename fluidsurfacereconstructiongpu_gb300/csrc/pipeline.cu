@@ -1,0 +1,685 @@
+// Frame orchestration and the fsr_* C ABI (include/fsr.h).
+//
+// One frame is one queue of kernels on the caller's stream: spatial hashing
+// (key + stable radix sort + ranges), surface cells, narrow band (bitset +
+// rank directory + band list), field, marching cubes (classify, two scans,
+// valid-cube list, generation).  Sizes the reference reads back after every
+// scan (ReconstructionCUDA.cu:1164-1171) stay on the device in a Counters
+// block; the host reads that block once at the end of the frame.  When a
+// pooled buffer turned out too small the frame is re-queued with the grown
+// capacities (only the first frames of a new workload pay for that).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fsr.h"
+#include "fsr_internal.h"
+#include "kernels.h"
+#include "primitives.h"
+
+namespace fsr {
+
+// ------------------------------------------------------------ grid derivation
+// ReconstructorGPU.cpp:237-268 (spatial grid: bbox grown by one cell,
+// res = uint((max - min) / cs + 1) in FP32) and :99-105 (scalar grid: cell
+// cs / ratio over the same box).
+bool derive_grids(const fsr_frame_header& hdr, const fsr_params& p, Grid& sp, Grid& sc, float* sp_max,
+                  uint64_t& C, uint64_t& V)
+{
+    const volatile float h = hdr.kernel_radius;  // volatile: keep every step in FP32
+    const float cs = h * p.cell_size_scale;
+    if (!(cs > 0.0f) || p.grid_ratio == 0 || !std::isfinite(cs)) return false;
+    const float scs = cs / (float)p.grid_ratio;
+    C = 1;
+    V = 1;
+    for (int a = 0; a < 3; ++a) {
+        const volatile float mn = hdr.bbox_min[a] - cs;
+        const volatile float mx = hdr.bbox_max[a] + cs;
+        const volatile float d = mx - mn;
+        const volatile float rs = d / cs + 1.0f;
+        const volatile float rv = d / scs + 1.0f;
+        if (!(rs >= 1.0f && rs < 4294967296.0f) || !(rv >= 2.0f && rv < 4294967296.0f)) return false;
+        sp.min[a] = mn;
+        sc.min[a] = mn;
+        sp.res[a] = (uint32_t)rs;
+        sc.res[a] = (uint32_t)rv;
+        if (sp_max) sp_max[a] = mx;
+        C *= sp.res[a];
+        V *= sc.res[a];
+    }
+    sp.cs = cs;
+    sc.cs = scs;
+    sp.pad = sc.pad = 0;
+    return true;
+}
+
+// Largest float t with (double)t < 1.5 * (double)h: dist <= t <=> the
+// reference's `dist < h * 1.5` evaluated in double (cu:587).
+float band_threshold(float h)
+{
+    const double t = (double)h * 1.5;
+    float f = (float)t;
+    if ((double)f >= t) f = std::nextafterf(f, 0.0f);
+    return f;
+}
+
+uint32_t bits_for(uint64_t c)
+{
+    uint32_t b = 0;
+    while (b < 32 && (1ull << b) < c) ++b;
+    return b;
+}
+
+}  // namespace fsr
+
+using namespace fsr;
+
+namespace {
+
+fsr_status fail(fsr_handle* h, fsr_status st, const char* fmt, ...)
+{
+    if (h) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        h->last_error = buf;
+    }
+    return st;
+}
+
+fsr_status cuda_fail(fsr_handle* h, cudaError_t e, const char* where)
+{
+    return fail(h, e == cudaErrorMemoryAllocation ? FSR_ERR_OUT_OF_MEMORY : FSR_ERR_CUDA, "%s: %s (%d)", where,
+                cudaGetErrorString(e), (int)e);
+}
+
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return cuda_fail(h, e_, #call);       \
+    } while (0)
+
+bool valid_params(const fsr_params& p)
+{
+    if (p.method > FSR_METHOD_AKINCI12) return false;
+    if (p.grid_ratio == 0 || !(p.cell_size_scale > 0.0f) || !std::isfinite(p.iso_value)) return false;
+    if (p.method == FSR_METHOD_YU13 && !(p.aniso_radius_over_h > 0.0f)) return false;
+    return true;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+// ------------------------------------------------------------ DevBuf
+
+cudaError_t DevBuf::ensure(size_t want)
+{
+    if (want <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    const size_t b = std::max<size_t>(want, 256);
+    cudaError_t e = cudaMalloc(&ptr, b);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        return e;
+    }
+    bytes = b;
+    return cudaSuccess;
+}
+
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+fsr_handle::~fsr_handle()
+{
+    DeviceGuard g(device);
+    for (DevBuf* b : all_buffers()) b->release();
+    if (pinned_ctr) cudaFreeHost(pinned_ctr);
+    for (auto& e : ev) {
+        if (e) cudaEventDestroy(e);
+    }
+    if (ev_start) cudaEventDestroy(ev_start);
+}
+
+std::vector<DevBuf*> fsr_handle::all_buffers()
+{
+    return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
+            &surf,   &invol,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &mesh_pos, &mesh_nrm, &pflags, &ctr};
+}
+
+// ------------------------------------------------------------ frame
+
+namespace fsr {
+
+fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_xyz, const float* d_den,
+                     uint64_t n64, cudaStream_t st)
+{
+    const fsr_params& p = h->params;
+    if (n64 >= 0xFFFFFFFFull) return fail(h, FSR_ERR_TOO_LARGE, "too many particles: %llu", (unsigned long long)n64);
+    const uint32_t n = (uint32_t)n64;
+    if (!(hdr.kernel_radius > 0.0f) || !std::isfinite(hdr.kernel_radius))
+        return fail(h, FSR_ERR_INVALID_ARGUMENT, "kernel radius must be positive");
+    Grid sp{}, sc{};
+    uint64_t C = 0, V = 0;
+    if (!derive_grids(hdr, p, sp, sc, nullptr, C, V))
+        return fail(h, FSR_ERR_INVALID_ARGUMENT, "invalid grid (bounding box, kernel radius or ratio)");
+    if (C >= 0xFFFFFFFFull || V >= 0xFFFFFFFFull)
+        return fail(h, FSR_ERR_TOO_LARGE, "grid too large: %llu cells, %llu vertices", (unsigned long long)C,
+                    (unsigned long long)V);
+    const uint32_t nwords = (uint32_t)((V + 31) / 32);
+    const bool yu13 = p.method == FSR_METHOD_YU13;
+    const bool akinci = p.method == FSR_METHOD_AKINCI12;
+    const bool keep = (p.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
+    const bool timing = (p.flags & FSR_FLAG_STAGE_TIMING) != 0;
+    const uint32_t nn = std::max<uint32_t>(n, 1);
+
+    // capacities of the device-sized arrays
+    if (h->cap_band == 0) h->cap_band = (uint32_t)std::min<uint64_t>(V, std::max<uint64_t>(1u << 20, 24ull * n));
+    if (h->cap_valid == 0) h->cap_valid = std::max<uint32_t>(1u << 18, h->cap_band / 4);
+    if (h->cap_mesh == 0) h->cap_mesh = std::max<uint32_t>(1u << 20, 4u * h->cap_valid);
+
+    CK(h->keys0.ensure(4ull * nn));
+    CK(h->vals0.ensure(4ull * nn));
+    CK(h->keys1.ensure(4ull * nn));
+    CK(h->vals1.ensure(4ull * nn));
+    CK(h->radix_tmp.ensure(4ull * radix_scratch_words(nn)));
+    CK(h->sorted.ensure(16ull * nn));
+    CK(h->ranges.ensure(8ull * C));
+    CK(h->occ.ensure(C));
+    CK(h->surf.ensure(C));
+    CK(h->bits.ensure(4ull * nwords + 4));
+    CK(h->prefix.ensure(4ull * nwords + 4));
+    CK(h->ctr.ensure(sizeof(Counters)));
+    if (yu13) {
+        CK(h->invol.ensure(C));
+        CK(h->mean.ensure(16ull * nn));
+        CK(h->smoothed.ensure(16ull * nn));
+        CK(h->grec.ensure(64ull * nn));
+    }
+    if (akinci) CK(h->psurf.ensure(nn));
+    if (keep) CK(h->pflags.ensure(4ull * nn));
+    if (!h->pinned_ctr) CK(cudaMallocHost(&h->pinned_ctr, sizeof(Counters)));
+    if (timing && !h->ev_start) {
+        CK(cudaEventCreate(&h->ev_start));
+        for (auto& e : h->ev) CK(cudaEventCreate(&e));
+    }
+
+    const KernelCtx kc{st, h->num_sms};
+    Counters* ctr = (Counters*)h->ctr.ptr;
+    const float h_r = hdr.kernel_radius;
+    const float h2 = h_r * h_r;
+
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        const uint64_t scan_words =
+            std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
+        CK(h->scan_tmp.ensure(4ull * scan_words));
+        CK(h->sv.ensure(4ull * h->cap_band));
+        CK(h->phi.ensure(4ull * h->cap_band));
+        CK(h->mc.ensure(4ull * h->cap_band));
+        CK(h->vofs.ensure(4ull * h->cap_band));
+        CK(h->qpos.ensure(4ull * h->cap_band));
+        CK(h->valid.ensure(4ull * h->cap_valid));
+        CK(h->mesh_pos.ensure(12ull * h->cap_mesh));
+        CK(h->mesh_nrm.ensure(12ull * h->cap_mesh));
+
+        auto mark = [&](int stage) {
+            if (timing) cudaEventRecord(h->ev[stage], st);
+        };
+        if (timing) cudaEventRecord(h->ev_start, st);
+
+        CK(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
+        CK(cudaMemsetAsync(h->ranges.ptr, 0xFF, 8ull * C, st));
+        CK(cudaMemsetAsync(h->occ.ptr, 0, C, st));
+        CK(cudaMemsetAsync(h->bits.ptr, 0, 4ull * nwords + 4, st));
+
+        // ---- spatial hashing (ReconstructorGPU.cpp:292-313)
+        uint32_t* k0 = (uint32_t*)h->keys0.ptr;
+        uint32_t* v0 = (uint32_t*)h->vals0.ptr;
+        uint32_t* k1 = (uint32_t*)h->keys1.ptr;
+        uint32_t* v1 = (uint32_t*)h->vals1.ptr;
+        launch_hash(kc, d_xyz, n, sp, k0, v0, ctr);
+        cudaError_t se = cudaSuccess;
+        const int which = radix_sort_pairs(k0, v0, k1, v1, n, bits_for(C), (uint32_t*)h->radix_tmp.ptr, st, &se);
+        if (se != cudaSuccess) return cuda_fail(h, se, "radix sort");
+        const uint32_t* skeys = which ? k1 : k0;
+        const uint32_t* perm = which ? v1 : v0;
+        h->perm_ptr = perm;
+        h->skeys_ptr = skeys;
+        mark(0);
+        float4* sorted = (float4*)h->sorted.ptr;
+        uint2* ranges = (uint2*)h->ranges.ptr;
+        uint8_t* occ = (uint8_t*)h->occ.ptr;
+        launch_ranges_gather(kc, skeys, perm, n, d_xyz, d_den, sorted, ranges, occ);
+        mark(1);
+
+        // ---- surface cells / particles
+        uint8_t* surf = (uint8_t*)h->surf.ptr;
+        uint8_t* psurf = akinci ? (uint8_t*)h->psurf.ptr : nullptr;
+        if (akinci) {
+            launch_colorfield(kc, sorted, n, ranges, sp, h_r, h2, hdr.particle_mass, psurf);
+        } else {
+            launch_surface_cells(kc, sp, occ, surf);
+            if (yu13) launch_involved_cells(kc, sp, occ, surf, (uint8_t*)h->invol.ptr);
+        }
+        if (keep) launch_particle_flags(kc, skeys, surf, psurf, n, (uint32_t*)h->pflags.ptr);
+        mark(2);
+
+        // ---- narrow band
+        uint32_t* bits = (uint32_t*)h->bits.ptr;
+        uint32_t* prefix = (uint32_t*)h->prefix.ptr;
+        launch_band_stamp(kc, sorted, skeys, surf, psurf, n, sc, band_threshold(h_r), bits, ctr);
+        mark(3);
+        CK(scan_u32(bits, prefix, nwords, nullptr, nwords, &ctr->n_band, ScanInput::kPopcount,
+                    (uint32_t*)h->scan_tmp.ptr, st));
+        uint32_t* sv = (uint32_t*)h->sv.ptr;
+        launch_band_list(kc, bits, prefix, nwords, sv, h->cap_band, ctr);
+        mark(4);
+
+        // ---- field
+        float* phi = (float*)h->phi.ptr;
+        if (yu13) {
+            const float R = h_r * p.aniso_radius_over_h;
+            launch_smooth(kc, sorted, n, ranges, sp, R, p.smoothing_lambda, hdr.particle_mass, (float4*)h->mean.ptr,
+                          (float4*)h->smoothed.ptr);
+            mark(5);
+            CovArgs ca{};
+            ca.sp = sp;
+            ca.sorted = sorted;
+            ca.mean = (const float4*)h->mean.ptr;
+            ca.smoothed = (const float4*)h->smoothed.ptr;
+            ca.ranges = ranges;
+            ca.skeys = skeys;
+            ca.invol = (const uint8_t*)h->invol.ptr;
+            ca.grec = (float4*)h->grec.ptr;
+            ca.n = n;
+            ca.R = R;
+            ca.h = h_r;
+            ca.h2 = h2;
+            ca.h_inv = (float)(1.0 / (double)h_r);
+            ca.mass = hdr.particle_mass;
+            ca.sigma = 315.0f / (64.0f * 3.1415926535898f);
+            ca.min_neighbors = p.min_neighbors;
+            launch_cov(kc, ca, ctr);
+            mark(6);
+            AnisoFieldArgs fa{};
+            fa.sp = sp;
+            fa.sc = sc;
+            fa.smoothed = (const float4*)h->smoothed.ptr;
+            fa.grec = (const float4*)h->grec.ptr;
+            fa.ranges = ranges;
+            fa.invol = (const uint8_t*)h->invol.ptr;
+            fa.occ = occ;
+            fa.sv = sv;
+            fa.phi = phi;
+            fa.sigma = ca.sigma;
+            fa.cap = h->cap_band;
+            launch_field_aniso(kc, fa, ctr);
+        } else {
+            mark(5);
+            mark(6);
+            IsoFieldArgs fa{};
+            fa.sp = sp;
+            fa.sc = sc;
+            fa.sorted = sorted;
+            fa.ranges = ranges;
+            fa.sv = sv;
+            fa.phi = phi;
+            fa.h2 = h2;
+            fa.inv_h2 = 1.0f / h2;
+            fa.rp = hdr.particle_radius;
+            fa.cap = h->cap_band;
+            launch_field_iso(kc, p.method == FSR_METHOD_TC01 ? Field::kTC01 : Field::kZB05, fa, ctr);
+        }
+        mark(7);
+
+        // ---- marching cubes
+        McArgs ma{};
+        ma.sc = sc;
+        ma.band = BandView{bits, prefix, phi};
+        ma.sv = sv;
+        ma.mc = (uint32_t*)h->mc.ptr;
+        ma.vofs = (const uint32_t*)h->vofs.ptr;
+        ma.qpos = (const uint32_t*)h->qpos.ptr;
+        ma.valid = (uint32_t*)h->valid.ptr;
+        ma.out_pos = (float*)h->mesh_pos.ptr;
+        ma.out_nrm = (float*)h->mesh_nrm.ptr;
+        ma.iso = p.iso_value;
+        ma.fill = yu13 ? __builtin_bit_cast(float, 0x64646464u) : 0.0f;  // memset values (Yu13.cpp:264, ZB05.cpp:324)
+        ma.host_mc = akinci ? 1 : 0;
+        ma.cap_band = h->cap_band;
+        ma.cap_valid = h->cap_valid;
+        ma.cap_mesh = h->cap_mesh;
+        launch_mc_classify(kc, ma, ctr);
+        mark(8);
+        CK(scan_u32(ma.mc, (uint32_t*)h->vofs.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_mesh_verts,
+                    ScanInput::kLowByte, (uint32_t*)h->scan_tmp.ptr, st));
+        CK(scan_u32(ma.mc, (uint32_t*)h->qpos.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_valid,
+                    ScanInput::kLowByteNonzero, (uint32_t*)h->scan_tmp.ptr, st));
+        launch_valid_list(kc, ma, ctr);
+        mark(9);
+        launch_mc_generate(kc, ma, ctr);
+        mark(10);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->pinned_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+        mark(11);
+        CK(cudaStreamSynchronize(st));
+
+        const Counters& hc = *h->pinned_ctr;
+        if (hc.out_of_grid)
+            return fail(h, FSR_ERR_OUT_OF_GRID, "%u particle(s) outside the expanded bounding box", hc.out_of_grid);
+        if (hc.overflow) {
+            if (hc.overflow & 1u) h->cap_band = (uint32_t)std::min<uint64_t>(V, (uint64_t)hc.need_band * 5 / 4 + 1024);
+            if (hc.overflow & 2u) h->cap_valid = std::min<uint32_t>(h->cap_band, hc.need_valid + hc.need_valid / 4 + 1024);
+            if (hc.overflow & 4u)
+                h->cap_mesh = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)hc.need_mesh * 5 / 4 + 4096);
+            if (hc.overflow & 1u) {
+                // a band overflow also invalidated the later stages' sizes
+                h->cap_valid = std::max<uint32_t>(h->cap_valid, std::min<uint32_t>(h->cap_band, h->cap_band / 4));
+            }
+            h->stats.n_retries++;
+            continue;
+        }
+        // stats
+        fsr_stats& s = h->stats;
+        s.n_particles = n;
+        s.n_cells = C;
+        s.n_grid_vertices = V;
+        s.n_surface_particles = hc.n_surface;
+        s.n_involved_particles = hc.n_involved;
+        s.n_band_vertices = hc.n_band;
+        s.n_valid_cubes = hc.n_valid;
+        s.n_mesh_vertices = hc.n_mesh_verts;
+        s.n_fp64_fallbacks = hc.n_fp64;
+        for (int a = 0; a < 3; ++a) {
+            s.spatial_res[a] = sp.res[a];
+            s.scalar_res[a] = sc.res[a];
+        }
+        if (timing) {
+            float prev = 0.f;
+            for (int i = 0; i < FSR_NUM_STAGES; ++i) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, h->ev_start, h->ev[i]);
+                s.stage_ms[i] = ms - prev;
+                prev = ms;
+            }
+            s.total_ms = prev;
+        }
+        h->frame_ready = true;
+        h->grid_sp = sp;
+        h->grid_sc = sc;
+        h->n_last = n;
+        h->C_last = C;
+        h->V_last = V;
+        return FSR_OK;
+    }
+    return fail(h, FSR_ERR_OUT_OF_MEMORY, "capacity growth did not converge");
+}
+
+}  // namespace fsr
+
+// ------------------------------------------------------------ C ABI
+
+extern "C" {
+
+uint32_t fsr_abi_version(void) { return FSR_ABI_VERSION; }
+
+const char* fsr_build_info(void)
+{
+    return "fsr_gb300 abi=1 arch=sm_103a";
+}
+
+fsr_status fsr_default_params(uint32_t method, fsr_params* out)
+{
+    if (!out || method > FSR_METHOD_AKINCI12) return FSR_ERR_INVALID_ARGUMENT;
+    fsr_params p{};
+    p.method = method;
+    p.smoothing_lambda = 0.5f;
+    p.aniso_radius_over_h = 2.0f;
+    p.min_neighbors = 25;
+    p.flags = 0;
+    switch (method) {
+    case FSR_METHOD_ZB05:  // ReconstructorGPUOursZB05.cpp:85-97
+    case FSR_METHOD_AKINCI12:  // ReconstructorGPUAkinci12.cpp:93-106
+        p.iso_value = -0.0001f;
+        p.grid_ratio = 2;
+        p.cell_size_scale = 1.0f;
+        break;
+    case FSR_METHOD_TC01:  // no reference caller: ZB05's grid, iso on the TC01 range [0, 1/4]
+        p.iso_value = 0.25f;
+        p.grid_ratio = 2;
+        p.cell_size_scale = 1.0f;
+        break;
+    case FSR_METHOD_YU13:  // ReconstructorGPUOursYu13.cpp:78-99, anisotropic radius 2h at :21
+        p.iso_value = 0.0f;
+        p.grid_ratio = 3;
+        p.cell_size_scale = 1.3f;
+        break;
+    }
+    *out = p;
+    return FSR_OK;
+}
+
+fsr_status fsr_create(const fsr_params* params, int device, fsr_handle** out)
+{
+    if (!params || !out) return FSR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!valid_params(*params)) return FSR_ERR_INVALID_ARGUMENT;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return FSR_ERR_CUDA;
+    }
+    fsr_handle* h = new (std::nothrow) fsr_handle();
+    if (!h) return FSR_ERR_OUT_OF_MEMORY;
+    h->params = *params;
+    h->device = device;
+    DeviceGuard g(device);
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (h->num_sms <= 0) h->num_sms = 1;
+    upload_mc_tables(0);
+    cudaError_t e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) {
+        delete h;
+        return FSR_ERR_CUDA;
+    }
+    *out = h;
+    return FSR_OK;
+}
+
+void fsr_destroy(fsr_handle* h) { delete h; }
+
+fsr_status fsr_set_params(fsr_handle* h, const fsr_params* params)
+{
+    if (!h || !params) return FSR_ERR_INVALID_ARGUMENT;
+    if (!valid_params(*params)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "invalid parameters");
+    h->params = *params;
+    h->frame_ready = false;
+    return FSR_OK;
+}
+
+const char* fsr_last_error(const fsr_handle* h) { return h ? h->last_error.c_str() : "null handle"; }
+
+fsr_status fsr_reconstruct(fsr_handle* h, const fsr_frame_header* hdr, const float* d_xyz, const float* d_density,
+                           uint64_t n, void* stream)
+{
+    if (!h || !hdr) return FSR_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!d_xyz || !d_density)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
+    DeviceGuard g(h->device);
+    h->frame_ready = false;
+    return run_frame(h, *hdr, d_xyz, d_density, n, (cudaStream_t)stream);
+}
+
+fsr_status fsr_reconstruct_host(fsr_handle* h, const fsr_frame_header* hdr, const float* xyz, const float* density,
+                                uint64_t n, float* out_pos, float* out_nrm, uint64_t capacity, uint64_t* n_vertices,
+                                void* stream)
+{
+    if (!h || !hdr || !n_vertices) return FSR_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!xyz || !density)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
+    DeviceGuard g(h->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint64_t nn = std::max<uint64_t>(n, 1);
+    CK(h->in_xyz.ensure(12ull * nn));
+    CK(h->in_den.ensure(4ull * nn));
+    if (n) {
+        CK(cudaMemcpyAsync(h->in_xyz.ptr, xyz, 12ull * n, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->in_den.ptr, density, 4ull * n, cudaMemcpyHostToDevice, st));
+    }
+    h->frame_ready = false;
+    fsr_status s = run_frame(h, *hdr, (const float*)h->in_xyz.ptr, (const float*)h->in_den.ptr, n, st);
+    if (s != FSR_OK) return s;
+    const uint64_t nv = h->stats.n_mesh_vertices;
+    *n_vertices = nv;
+    if (nv > capacity) return fail(h, FSR_ERR_CAPACITY, "mesh has %llu vertices, buffer holds %llu",
+                                   (unsigned long long)nv, (unsigned long long)capacity);
+    if (nv) {
+        if (!out_pos || !out_nrm) return fail(h, FSR_ERR_INVALID_ARGUMENT, "null mesh output");
+        CK(cudaMemcpyAsync(out_pos, h->mesh_pos.ptr, 12ull * nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(out_nrm, h->mesh_nrm.ptr, 12ull * nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return FSR_OK;
+}
+
+fsr_status fsr_mesh_device(fsr_handle* h, const float** d_pos, const float** d_nrm, uint64_t* n_vertices)
+{
+    if (!h || !d_pos || !d_nrm || !n_vertices) return FSR_ERR_INVALID_ARGUMENT;
+    if (!h->frame_ready) return fail(h, FSR_ERR_NOT_READY, "no frame reconstructed");
+    *d_pos = (const float*)h->mesh_pos.ptr;
+    *d_nrm = (const float*)h->mesh_nrm.ptr;
+    *n_vertices = h->stats.n_mesh_vertices;
+    return FSR_OK;
+}
+
+fsr_status fsr_copy_mesh(fsr_handle* h, float* out_pos, float* out_nrm, uint64_t capacity, uint64_t* n_vertices)
+{
+    if (!h || !n_vertices) return FSR_ERR_INVALID_ARGUMENT;
+    if (!h->frame_ready) return fail(h, FSR_ERR_NOT_READY, "no frame reconstructed");
+    DeviceGuard g(h->device);
+    const uint64_t nv = h->stats.n_mesh_vertices;
+    *n_vertices = nv;
+    if (nv > capacity) return fail(h, FSR_ERR_CAPACITY, "mesh buffer too small");
+    if (nv) {
+        if (!out_pos || !out_nrm) return FSR_ERR_INVALID_ARGUMENT;
+        CK(cudaMemcpy(out_pos, h->mesh_pos.ptr, 12ull * nv, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(out_nrm, h->mesh_nrm.ptr, 12ull * nv, cudaMemcpyDeviceToHost));
+    }
+    return FSR_OK;
+}
+
+fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out)
+{
+    if (!h || !out) return FSR_ERR_INVALID_ARGUMENT;
+    *out = h->stats;
+    return FSR_OK;
+}
+
+fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes, uint64_t* bytes_needed)
+{
+    if (!h) return FSR_ERR_INVALID_ARGUMENT;
+    if (!h->frame_ready) return fail(h, FSR_ERR_NOT_READY, "no frame reconstructed");
+    DeviceGuard g(h->device);
+    const uint64_t n = h->n_last, C = h->C_last;
+    const fsr_stats& s = h->stats;
+    const bool yu13 = h->params.method == FSR_METHOD_YU13;
+    const bool keep = (h->params.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
+    uint64_t need = 0;
+    switch (which) {
+    case FSR_DBG_SORT_PERM: need = 4 * n; break;
+    case FSR_DBG_SORTED_XYZ: need = 12 * n; break;
+    case FSR_DBG_CELL_RANGES: need = 8 * C; break;
+    case FSR_DBG_SURFACE_FLAGS: need = keep ? 4 * n : 0; break;
+    case FSR_DBG_INVOLVED_COUNTS: need = yu13 ? 4 * C : 0; break;
+    case FSR_DBG_BAND_VERTICES:
+    case FSR_DBG_FIELD:
+    case FSR_DBG_MC_INFO: need = 4 * s.n_band_vertices; break;
+    case FSR_DBG_VALID_CUBES: need = 4 * s.n_valid_cubes; break;
+    case FSR_DBG_MEAN:
+    case FSR_DBG_SMOOTHED: need = yu13 ? 12 * n : 0; break;
+    case FSR_DBG_G: need = yu13 ? 36 * n : 0; break;
+    default: return fail(h, FSR_ERR_INVALID_ARGUMENT, "unknown debug array %u", which);
+    }
+    if (bytes_needed) *bytes_needed = need;
+    if (!dst) return FSR_OK;
+    if (dst_bytes < need) return fail(h, FSR_ERR_CAPACITY, "debug buffer too small");
+    if (need == 0) return FSR_OK;
+    auto copy4 = [&](const DevBuf& b, size_t stride_floats, size_t take, size_t count, float* out) -> cudaError_t {
+        std::vector<float> tmp(stride_floats * count);
+        cudaError_t e = cudaMemcpy(tmp.data(), b.ptr, 4 * tmp.size(), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+        for (size_t i = 0; i < count; ++i)
+            for (size_t k = 0; k < take; ++k) out[take * i + k] = tmp[stride_floats * i + k];
+        return cudaSuccess;
+    };
+    switch (which) {
+    case FSR_DBG_SORT_PERM: CK(cudaMemcpy(dst, h->perm_ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_SORTED_XYZ: CK(copy4(h->sorted, 4, 3, n, (float*)dst)); break;
+    case FSR_DBG_CELL_RANGES: CK(cudaMemcpy(dst, h->ranges.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_SURFACE_FLAGS: CK(cudaMemcpy(dst, h->pflags.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_INVOLVED_COUNTS: {
+        std::vector<uint8_t> inv(C);
+        std::vector<uint32_t> rg(2 * C);
+        CK(cudaMemcpy(inv.data(), h->invol.ptr, C, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rg.data(), h->ranges.ptr, 8 * C, cudaMemcpyDeviceToHost));
+        uint32_t* o = (uint32_t*)dst;
+        for (uint64_t c = 0; c < C; ++c) o[c] = inv[c] ? rg[2 * c + 1] - rg[2 * c] : 0u;
+        break;
+    }
+    case FSR_DBG_BAND_VERTICES: CK(cudaMemcpy(dst, h->sv.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_FIELD: CK(cudaMemcpy(dst, h->phi.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_MC_INFO: {
+        CK(cudaMemcpy(dst, h->mc.ptr, need, cudaMemcpyDeviceToHost));
+        uint32_t* o = (uint32_t*)dst;
+        for (uint64_t i = 0; i < s.n_band_vertices; ++i) {
+            const uint32_t nv = o[i] & 0xFFu;
+            o[i] = (o[i] >> 8) | (nv << 8) | ((nv ? 1u : 0u) << 16);
+        }
+        break;
+    }
+    case FSR_DBG_VALID_CUBES: CK(cudaMemcpy(dst, h->valid.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_MEAN: CK(copy4(h->mean, 4, 3, n, (float*)dst)); break;
+    case FSR_DBG_SMOOTHED: CK(copy4(h->smoothed, 4, 3, n, (float*)dst)); break;
+    case FSR_DBG_G: {
+        std::vector<float> tmp(16 * n);
+        CK(cudaMemcpy(tmp.data(), h->grec.ptr, 64 * n, cudaMemcpyDeviceToHost));
+        float* o = (float*)dst;
+        for (uint64_t i = 0; i < n; ++i) {
+            const float* r = &tmp[16 * i];
+            const float g[9] = {r[4], r[5], r[6], r[8], r[9], r[10], r[12], r[13], r[14]};
+            for (int k = 0; k < 9; ++k) o[9 * i + k] = g[k];
+        }
+        break;
+    }
+    }
+    return FSR_OK;
+}
+
+}  // extern "C"

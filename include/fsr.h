@@ -1,0 +1,185 @@
+/*
+ * fsr.h - C ABI of the GB300 particle-to-mesh surface reconstruction library
+ * (libfsr_gb300.so).  Plain C types only; every call returns an fsr_status
+ * and never exits the process.
+ *
+ * The frame-level calls replace the reference's per-frame reconstruct path:
+ *   ReconstructorGPU::reconstruct / beginFrame / frameMove / endFrame
+ *     (FluidSurfaceReconstruction/GPU/ReconstructorGPU.cpp:25-148)
+ *   and the stage sequences of onFrameMove in
+ *     ReconstructorGPUOursZB05.cpp:22-78, ReconstructorGPUOursYu13.cpp:24-63,
+ *     ReconstructorGPUAkinci12.cpp:34-84.
+ * The kernel-level entry points the reference's host classes bind
+ * (ReconstructionCUDA.cuh:17-248) are declared in fsr_compat.h.
+ *
+ * Threading: a handle is used by one host thread at a time.  Work is queued
+ * on the stream passed in (NULL = the legacy default stream); calls that
+ * return host-visible results synchronise that stream.
+ */
+#ifndef FSR_GB300_H
+#define FSR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSR_ABI_VERSION 1
+
+typedef enum fsr_status {
+    FSR_OK = 0,
+    FSR_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size or parameter */
+    FSR_ERR_OUT_OF_GRID = 2,      /* a particle lies outside the expanded bounding box */
+    FSR_ERR_CUDA = 3,             /* a CUDA runtime call failed; see fsr_last_error */
+    FSR_ERR_OUT_OF_MEMORY = 4,    /* device or host allocation failed */
+    FSR_ERR_IO = 5,               /* .xyz / .obj file could not be read or written */
+    FSR_ERR_FORMAT = 6,           /* malformed .xyz file */
+    FSR_ERR_CAPACITY = 7,         /* a caller-provided output buffer is too small */
+    FSR_ERR_TOO_LARGE = 8,        /* grid or particle count beyond the 32-bit index space */
+    FSR_ERR_NOT_READY = 9         /* no frame has been reconstructed on this handle yet */
+} fsr_status;
+
+/* Field / reconstructor families of the reference. */
+typedef enum fsr_method {
+    FSR_METHOD_ZB05 = 0,     /* ReconstructorGPUOursZB05: flag-grid surface + ZB05 field */
+    FSR_METHOD_TC01 = 1,     /* same pipeline with the TC01 field (cu:178-227) */
+    FSR_METHOD_YU13 = 2,     /* ReconstructorGPUOursYu13: anisotropic field */
+    FSR_METHOD_AKINCI12 = 3  /* ReconstructorGPUAkinci12: colour-field surface + ZB05 */
+} fsr_method;
+
+/* Reconstructor settings.  fsr_default_params fills the values each
+ * reference reconstructor sets in onInitialization (ZB05.cpp:85-97,
+ * Yu13.cpp:78-99 and :21, Akinci12.cpp:93-106). */
+typedef struct fsr_params {
+    uint32_t method;             /* fsr_method */
+    float iso_value;             /* SimParam.isoValue */
+    uint32_t grid_ratio;         /* SimParam.scSpGridResRatio: spatial cell / scalar cell */
+    float cell_size_scale;       /* SimParam.spatialCellSizeScale: spatial cell / h */
+    float smoothing_lambda;      /* SimParam.lambdaForSmoothed (Yu13) */
+    float aniso_radius_over_h;   /* SimParam.anisotropicRadius / h (Yu13: 2) */
+    uint32_t min_neighbors;      /* SimParam.minNumNeighbors (Yu13: 25) */
+    uint32_t flags;              /* FSR_FLAG_* */
+} fsr_params;
+
+/* Keep per-stage intermediates for fsr_debug_fetch (parity tests). */
+#define FSR_FLAG_KEEP_INTERMEDIATES 0x1u
+/* Record per-stage CUDA event times (fsr_stats.stage_ms). */
+#define FSR_FLAG_STAGE_TIMING 0x2u
+
+/* The .xyz header (data_format.txt:1-15; ReconstructorGPU.cpp:215-251). */
+typedef struct fsr_frame_header {
+    float bbox_min[3];
+    float bbox_max[3];
+    float kernel_radius;     /* h */
+    float particle_radius;
+    float particle_mass;
+} fsr_frame_header;
+
+#define FSR_NUM_STAGES 12
+
+typedef struct fsr_stats {
+    uint64_t n_particles;
+    uint64_t n_cells;              /* spatial cells C */
+    uint64_t n_grid_vertices;      /* scalar-grid vertices V */
+    uint64_t n_surface_particles;
+    uint64_t n_involved_particles; /* Yu13: particles that receive a G matrix */
+    uint64_t n_band_vertices;      /* B */
+    uint64_t n_valid_cubes;        /* Q */
+    uint64_t n_mesh_vertices;      /* 3 x triangles */
+    uint32_t spatial_res[3];
+    uint32_t scalar_res[3];
+    uint32_t n_fp64_fallbacks;     /* Yu13: eigen-solves redone in FP64 */
+    uint32_t n_retries;            /* frame re-runs after a capacity grow */
+    float stage_ms[FSR_NUM_STAGES];/* with FSR_FLAG_STAGE_TIMING */
+    float total_ms;
+} fsr_stats;
+
+typedef struct fsr_handle fsr_handle;
+
+/* Library identity: ABI version and the compiled GPU architecture. */
+uint32_t fsr_abi_version(void);
+const char* fsr_build_info(void);
+
+fsr_status fsr_default_params(uint32_t method, fsr_params* out);
+
+/* Creates a reconstructor bound to CUDA device `device`.  Device memory is
+ * pooled inside the handle and grows on demand; it is released by
+ * fsr_destroy. */
+fsr_status fsr_create(const fsr_params* params, int device, fsr_handle** out);
+void fsr_destroy(fsr_handle* h);
+fsr_status fsr_set_params(fsr_handle* h, const fsr_params* params);
+const char* fsr_last_error(const fsr_handle* h);
+
+/* One frame, inputs on the device: xyz = N x 3 float (x,y,z per particle,
+ * the reference's ParticlePosition array), density = N floats.  The inputs
+ * are read only.  The mesh stays on the device until the next frame:
+ * fsr_mesh_device / fsr_copy_mesh return it.  Synchronises `stream` once at
+ * the end to read the frame's sizes. */
+fsr_status fsr_reconstruct(fsr_handle* h, const fsr_frame_header* hdr, const float* d_xyz,
+                           const float* d_density, uint64_t n, void* stream);
+
+/* One frame end to end from host memory: copies the particles to the
+ * device, reconstructs, copies the triangle soup back (positions and
+ * normals, 3 floats per mesh vertex, 3 mesh vertices per triangle, in the
+ * reference's order).  *n_vertices receives the mesh vertex count; if it
+ * exceeds `capacity` nothing is copied and FSR_ERR_CAPACITY is returned. */
+fsr_status fsr_reconstruct_host(fsr_handle* h, const fsr_frame_header* hdr, const float* xyz,
+                                const float* density, uint64_t n, float* out_pos, float* out_nrm,
+                                uint64_t capacity, uint64_t* n_vertices, void* stream);
+
+/* Device pointers to the last frame's mesh (valid until the next frame). */
+fsr_status fsr_mesh_device(fsr_handle* h, const float** d_pos, const float** d_nrm,
+                           uint64_t* n_vertices);
+fsr_status fsr_copy_mesh(fsr_handle* h, float* out_pos, float* out_nrm, uint64_t capacity,
+                         uint64_t* n_vertices);
+
+fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out);
+
+/* Intermediates of the last frame (requires FSR_FLAG_KEEP_INTERMEDIATES for
+ * the arrays marked *).  With dst == NULL only *bytes_needed is set. */
+typedef enum fsr_debug_array {
+    FSR_DBG_SORT_PERM = 0,       /* u32[N]  input index of each sorted particle */
+    FSR_DBG_SORTED_XYZ = 1,      /* f32[N*3] sorted positions */
+    FSR_DBG_CELL_RANGES = 2,     /* u32[C*2] {start,end}, 0xFFFFFFFF = empty */
+    FSR_DBG_SURFACE_FLAGS = 3,   /* u32[N]  surface particle flags (sorted order) */
+    FSR_DBG_INVOLVED_COUNTS = 4, /* u32[C]  Yu13 involved counts per cell */
+    FSR_DBG_BAND_VERTICES = 5,   /* u32[B]  band vertex ids, ascending */
+    FSR_DBG_FIELD = 6,           /* f32[B]  field at the band vertices */
+    FSR_DBG_MC_INFO = 7,         /* u32[B]  case | nverts << 8 | valid << 16 */
+    FSR_DBG_VALID_CUBES = 8,     /* u32[Q]  positions in the band list of valid cubes */
+    FSR_DBG_MEAN = 9,            /* f32[N*3] Yu13 weighted means (sorted order) */
+    FSR_DBG_SMOOTHED = 10,       /* f32[N*3] Yu13 smoothed positions */
+    FSR_DBG_G = 11               /* f32[N*9] Yu13 G matrices, row-major, sorted order (*) */
+} fsr_debug_array;
+
+fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes,
+                           uint64_t* bytes_needed);
+
+/* ---- file formats -------------------------------------------------- */
+
+/* Parses an .xyz file (data_format.txt; ReconstructorGPU.cpp:200-290).
+ * *xyz and *density are allocated with malloc; release them with
+ * fsr_free_host. */
+fsr_status fsr_read_xyz(const char* path, fsr_frame_header* hdr, float** xyz, float** density,
+                        uint64_t* n);
+void fsr_free_host(void* p);
+
+/* Writes a triangle soup as .obj: v lines, vn lines, then
+ * "f i//i i+1//i+1 i+2//i+2" per triangle (ReconstructorGPUOurs.cpp:58-99). */
+fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm,
+                         uint64_t n_vertices);
+
+/* File-driven frame loop of ReconstructorGPU::reconstruct (ReconstructorGPU.cpp:
+ * 25-79): frames [from, to) of directory + printf(pattern, frame) + ".xyz",
+ * each written to the same stem + ".obj" when write_obj != 0.  Per-frame
+ * milliseconds (hashing to mesh, the reference's timer scope) are stored in
+ * frame_ms[0 .. to-from) when frame_ms is not NULL. */
+fsr_status fsr_reconstruct_files(fsr_handle* h, const char* directory, const char* pattern,
+                                 uint32_t from, uint32_t to, int write_obj, double* frame_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

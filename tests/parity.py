@@ -1,0 +1,112 @@
+"""Shared GPU-vs-oracle comparison used by the parity tests and bench checks.
+
+Integer results (sort order, cell ranges, surface flags, involved counts,
+band vertices, MC cases, valid cubes, triangle counts) must equal the FP32
+oracle's.  The only exemption: marching-cubes cubes with a corner whose FP64
+field value lies within NEAR_ISO of the iso value, where a last-bit
+difference in summation order may legitimately flip the case; such cubes are
+counted and reported.  Field values, G matrices and mesh vertices are
+compared with the FP64 oracle within the stated tolerances.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+NEAR_ISO = 1e-6
+
+
+def field_tolerance(method: str, h: float, phi64: np.ndarray) -> np.ndarray:
+    """Absolute tolerance per band vertex: 1e-5 relative of the field's scale.
+    ZB05 is a distance (scale h); TC01 and the anisotropic field are sums of
+    O(1) kernel values (scale max(1, |phi|))."""
+    if method in ("zb05", "akinci"):
+        return 1e-5 * np.maximum(h, np.abs(phi64))
+    return 1e-5 * np.maximum(1.0, np.abs(phi64))
+
+
+def corner_ids(cubes: np.ndarray, res) -> np.ndarray:
+    rx, ry = res[0], res[0] * res[1]
+    off = np.array([0, rx * ry, rx * ry + rx, rx, 1, 1 + rx * ry, 1 + rx + rx * ry, 1 + rx], dtype=np.int64)
+    # corner order of ReconstructionCUDA.cuh:441-452, (dx, dy, dz) per corner
+    dx = np.array([0, 0, 0, 0, 1, 1, 1, 1])
+    dy = np.array([0, 0, 1, 1, 0, 0, 1, 1])
+    dz = np.array([0, 1, 1, 0, 0, 1, 1, 0])
+    off = dx + dy * rx + dz * ry
+    return cubes.astype(np.int64)[:, None] + off[None, :]
+
+
+def compare_frame(rec, o32, o64, method: str, h: float) -> dict:
+    """rec: api.Reconstructor after a frame with keep_intermediates=True."""
+    rep = {}
+    assert np.array_equal(rec.debug("perm"), o32.perm), "stable sort order differs"
+    assert np.array_equal(rec.debug("ranges"), o32.ranges), "cell ranges differ"
+    assert np.array_equal(rec.debug("sorted_xyz"), o32.pos), "sorted positions differ"
+    assert np.array_equal(rec.debug("surface_flags"), o32.sflag), "surface particle flags differ"
+    if method == "yu13":
+        assert np.array_equal(rec.debug("involved_counts"), o32.ninv), "involved counts differ"
+        assert np.array_equal(rec.debug("mean"), o32.mean32), "weighted means differ"
+        sm = rec.debug("smoothed")
+        assert np.allclose(sm, o64.smoothed, rtol=0, atol=1e-6), "smoothed positions"
+        G = rec.debug("G")[o32.inv]
+        G64 = o64.G
+        rel = np.linalg.norm(G - G64, axis=1) / np.linalg.norm(G64, axis=1)
+        rep["G_rel_max"] = float(rel.max()) if rel.size else 0.0
+        assert rep["G_rel_max"] <= 1e-5, f"G relative error {rep['G_rel_max']:.3e}"
+    sv = rec.debug("band")
+    assert np.array_equal(sv, o32.sv), "band vertices differ"
+    phi = rec.debug("field").astype(np.float64)
+    phi64 = o64.phi[o64.sv]
+    tol = field_tolerance(method, h, phi64)
+    err = np.abs(phi - phi64)
+    rep["field_abs_max"] = float(err.max()) if err.size else 0.0
+    rep["field_viol"] = int((err > tol).sum())
+    assert rep["field_viol"] == 0, f"{rep['field_viol']} field values beyond tolerance (max {err.max():.3e})"
+
+    # marching cubes
+    info = rec.debug("mc_info")
+    gcase, gnv, gvalid = info & 0xFF, (info >> 8) & 0xFF, (info >> 16) & 1
+    ovalid = o32.valid.astype(np.uint32)
+    res = o32.scalar.resolution
+    V = o32.scalar.count
+    inner = np.ones(sv.size, bool)
+    x = sv % res[0]
+    y = (sv // res[0]) % res[1]
+    z = sv // (res[0] * res[1])
+    inner &= (x < res[0] - 1) & (y < res[1] - 1) & (z < res[2] - 1)
+    corners = np.zeros((sv.size, 8), np.int64)
+    corners[inner] = corner_ids(sv[inner], res)
+    near = np.zeros(sv.size, bool)
+    near[inner] = np.any(np.abs(o64.phi[np.clip(corners[inner], 0, V - 1)] - o32.simparam.isoValue) < NEAR_ISO,
+                         axis=1)
+    rep["near_iso_cubes"] = int(near.sum())
+    mism = (gvalid != ovalid) & ~near
+    assert not mism.any(), f"{int(mism.sum())} valid-cube flags differ outside near-iso cubes"
+    if method != "akinci":
+        mism = (gnv != o32.nverts) & ~near
+        assert not mism.any(), f"{int(mism.sum())} vertex counts differ outside near-iso cubes"
+    vq = np.flatnonzero(ovalid)
+    ocase = np.zeros(sv.size, np.uint32)
+    if vq.size:
+        from oracle import pipeline as P
+        import ctypes
+        ocase[vq] = P.cube_cases("oracle32", o32, sv[vq])
+    mism = (gcase != ocase) & (ovalid == 1) & ~near
+    assert not mism.any(), f"{int(mism.sum())} MC case indices differ outside near-iso cubes"
+    mesh = rec.mesh()
+    rep["triangles"] = mesh.n_triangles
+    rep["triangles_oracle"] = o32.n_triangles
+    if rep["near_iso_cubes"] == 0:
+        assert mesh.n_triangles == o32.n_triangles, "triangle count differs"
+    same_topo = np.array_equal(gvalid, o64.valid.astype(np.uint32)) and (
+        method == "akinci" or np.array_equal(gnv, o64.nverts)) and mesh.positions.shape == o64.mesh_pos.shape
+    rep["mesh_compared"] = bool(same_topo)
+    if same_topo and mesh.positions.size:
+        scale = np.maximum(np.abs(o64.mesh_pos), 1.0)
+        perr = np.abs(mesh.positions - o64.mesh_pos) / scale
+        rep["vertex_rel_max"] = float(perr.max())
+        assert rep["vertex_rel_max"] <= 1e-5, f"mesh vertices off by {rep['vertex_rel_max']:.3e}"
+        finite = np.isfinite(o64.mesh_nrm).all(axis=1) & np.isfinite(mesh.normals).all(axis=1)
+        rep["normal_nonfinite"] = int((~finite).sum())
+        if finite.any():
+            rep["normal_abs_max"] = float(np.abs(mesh.normals[finite] - o64.mesh_nrm[finite]).max())
+    return rep
