@@ -1,0 +1,327 @@
+"""Benchmark: particles/s of one reconstruct frame on the GB300.
+
+Workload (default, the anisotropic 1M-particle frame): a 0.4 x 0.8 x 0.4
+dam-break column + droplet (R 0.08) + splash, 2^20 particles, particle
+radius r = 0.004, h = 4r; anisotropic (Yu13-family) field with lambda 0.9,
+neighbour radius 4r, spatial cell 1.25h and grid spacing 0.5r (ratio 10);
+seeded synthetic data.  A step is one whole frame: hashing -> sort ->
+surface -> band -> smoothing -> covariance/G -> field -> marching cubes ->
+mesh sizes read back.
+
+Output: one JSON line on rank 0 (see the keys below).  With
+``--impl reference`` the reference's own pipeline (its kernels compiled for
+the host CPU, OpenMP over the launch domains; the CPU oracle port where that
+build is absent) is timed on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # the anisotropic 1M frame (headline)
+    "aniso1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="yu13", smoothing_lambda=0.9,
+                    aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
+    # the same frame with the plain ZB05 path (grid spacing 0.5r: ratio 8 at cell = h)
+    "plain1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="zb05", grid_ratio=8),
+    # 32^3 lattice, ZB05, grid spacing 0.5r
+    "plain32k": dict(kind="lattice", n_side=32, r=0.0125, seed=1, method="zb05", grid_ratio=8),
+}
+METRIC = "particles/s recon (fwd) @1M aniso"
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def make_frame(w):
+    from fluidsurfacereconstructiongpu_gb300 import synthetic
+    if w["kind"] == "dam_break":
+        return synthetic.dam_break(w["n"], r=w["r"], seed=w["seed"])
+    return synthetic.lattice_cube(w["n_side"], w["r"], seed=w["seed"])
+
+
+def recon_kwargs(w):
+    keys = ("smoothing_lambda", "aniso_radius_over_h", "cell_size_scale", "grid_ratio", "iso")
+    return {k: w[k] for k in keys if k in w}
+
+
+def oracle_params(w, fr):
+    from oracle import pipeline as P
+    return P.FrameParams(method=w["method"], h=fr.h, particle_radius=fr.particle_radius, mass=fr.mass,
+                         iso=w.get("iso"), ratio=w.get("grid_ratio"), cell_scale=w.get("cell_size_scale"),
+                         lam=w.get("smoothing_lambda", 0.5),
+                         aniso_radius=(w["aniso_radius_over_h"] * fr.h if "aniso_radius_over_h" in w else None))
+
+
+def cpu_kind():
+    """The reference's kernels built for this host when present, else the port."""
+    from oracle import pipeline as P
+    if P.available("ref"):
+        try:
+            P.load("ref")
+            return "ref", "reference"
+        except OSError:
+            pass
+    return "oracle32", "port"
+
+
+def cpu_frame(w, fr, field_stride):
+    """One CPU frame; returns (seconds, description of the sample)."""
+    from oracle import pipeline as P
+    kind, label = cpu_kind()
+    threads = P.set_threads(kind, os.cpu_count() or 1)
+    times = {}
+    t0 = time.perf_counter()
+    P.run_frame(kind, fr.pos, fr.density, fr.bbox_min, fr.bbox_max, oracle_params(w, fr), times=times,
+                field_stride=field_stride)
+    wall = time.perf_counter() - t0
+    est = wall + times.get("_unsampled_extra", 0.0)
+    sample = (f"one full {fr.n}-particle frame, all stages; field evaluated at every {field_stride}-th band "
+              f"vertex and its time scaled by {field_stride}") if field_stride > 1 else \
+        f"one full {fr.n}-particle frame, all stages"
+    return est, label, threads, sample
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel_key):
+    """DRAM bytes per algorithmic byte of the kernel, from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(kernel_key)
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def run_reference(args, w, fr):
+    """--impl reference: the reference's pipeline on the host cores."""
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return
+    stride = args.cpu_field_stride
+    for _ in range(args.warmup):
+        cpu_frame(w, fr, max(stride, 8))
+    secs = []
+    label = threads = sample = None
+    for _ in range(args.steps):
+        s, label, threads, sample = cpu_frame(w, fr, stride)
+        secs.append(s)
+    t = float(np.mean(secs))
+    val = fr.n / t
+    line = {"metric": METRIC, "value": val, "unit": "particles/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break)",
+            "config": {"workload": args.workload, "particles": fr.n, "method": w["method"]}, "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": "particles/s", "cores": threads, "kind": label,
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="aniso1m")
+    ap.add_argument("--cpu-field-stride", type=int, default=4,
+                    help="CPU baseline: evaluate the field at every k-th band vertex and scale its time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+
+    if args.impl == "reference":
+        fr = make_frame(w)
+        run_reference(args, w, fr)
+        return
+
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api, _native
+
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w_rank = dict(w)
+    w_rank["seed"] = w["seed"] + rank  # replicas: independent frames of the same workload
+    fr = make_frame(w_rank)
+
+    # CPU baseline first (rank 0, N = 1), before any GPU work
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        s, label, threads, sample = cpu_frame(w, fr, args.cpu_field_stride)
+        cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample}
+
+    rec = api.Reconstructor(w["method"], local, stage_timing=True, **recon_kwargs(w))
+    hdr = api.header_of(fr)
+    xyz = torch.from_numpy(fr.pos).to(dev)
+    den = torch.from_numpy(fr.density).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    launches0 = None
+    for _ in range(args.warmup):
+        rec.reconstruct(xyz, den, hdr, stream)
+    st = rec.stats()
+    n_launch_per_frame = getattr(_native, "KERNELS_PER_FRAME", {}).get(w["method"])
+
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stage = np.zeros(_native.NUM_STAGES)
+    for k in range(args.steps):
+        flush.zero_()  # evict L2 between steps (outside the timed events)
+        starts[k].record(stream)
+        rec.reconstruct(xyz, den, hdr, stream)
+        ends[k].record(stream)
+        s = rec.stats()
+        stage += np.array(list(s.stage_ms))
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    t_step = float(np.mean(ms)) / 1e3
+    st = rec.stats()
+    stage /= args.steps
+    if pg:
+        tt = torch.tensor([t_step], dtype=torch.float64, device=dev)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = fr.n * world / t_step
+
+    # end to end through the host API: pinned inputs in, mesh out, every step
+    pin_xyz = torch.from_numpy(fr.pos).pin_memory()
+    pin_den = torch.from_numpy(fr.density).pin_memory()
+    nv = int(st.n_mesh_vertices)
+    cap = int(nv * 1.2) + 1024
+    out_pos = torch.empty((cap, 3), dtype=torch.float32).pin_memory()
+    out_nrm = torch.empty((cap, 3), dtype=torch.float32).pin_memory()
+    import ctypes
+    e2e_t = []
+    nvo = ctypes.c_uint64(0)
+    for k in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        rc = _native.lib.fsr_reconstruct_host(rec._h, ctypes.byref(hdr), pin_xyz.data_ptr(), pin_den.data_ptr(),
+                                              fr.n, out_pos.data_ptr(), out_nrm.data_ptr(), cap,
+                                              ctypes.byref(nvo), ctypes.c_void_p(stream.cuda_stream))
+        _native.check(rc, rec._h)
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_t.append(t1 - t0)
+    e2e_step = float(np.mean(e2e_t))
+    h2d = fr.n * 16
+    d2h = int(nvo.value) * 24 + 64
+
+    # roofline of the dominant kernel (the field stage)
+    field_ms = float(stage[7])
+    n_inv = int(st.n_involved_particles)
+    B = int(st.n_band_vertices)
+    alg_bytes = 16 * fr.n + 36 * n_inv + 8 * B  # smoothed particles + G read once, band ids read, field written
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (field_ms / 1e3) / 1e9
+    tr = committed_traffic(f"{w['method']}_field_bytes_per_band_vertex")
+    roofline = {"bound": "hbm", "kernel": "k_field_aniso" if w["method"] == "yu13" else "k_field_iso",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind, "traffic": (tr * B if tr else None),
+                "algorithmic_bytes": alg_bytes, "launch_ms": field_ms}
+
+    line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break, L2 flushed between steps)",
+            "config": {"workload": args.workload, "particles": fr.n, "method": w["method"],
+                       "band_vertices": B, "triangles": int(st.n_mesh_vertices) // 3,
+                       "scalar_grid": list(st.scalar_res), "l2": "flushed (256 MB write) between steps",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": fr.n / e2e_step, "unit": "particles/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": (int(st.n_kernel_launches) * args.steps if hasattr(st, "n_kernel_launches") else None),
+            "stage_ms": {n: round(float(v), 4) for n, v in zip(_native.STAGE_NAMES, stage)},
+            "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    rec.close()
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

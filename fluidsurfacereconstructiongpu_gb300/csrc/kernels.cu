@@ -7,6 +7,7 @@
 namespace fsr {
 
 __constant__ McConst c_mc;
+thread_local uint64_t g_launches = 0;
 
 void upload_mc_tables(cudaStream_t s)
 {
@@ -268,16 +269,19 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
                 }
                 for (uint32_t i = beg; i < end; ++i) {
                     const float4 q = __ldg(&a.sorted[i]);
-                    const float dx = vx - q.x, dy = vy - q.y, dz = vz - q.z;
+                    const float dx = q.x - vx, dy = q.y - vy, dz = q.z - vz;
                     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     if (F == Field::kZB05) {
+                        // weighted mean taken as an offset from the vertex:
+                        // |v - sum w p / sum w| = |sum w (p - v)| / sum w, the
+                        // same value with FP32 error relative to h, not to |p|
                         if (d2 < a.h2) {
                             const float u = 1.0f - d2 * a.inv_h2;
                             const float wt = u * u * u;
                             ws += wt;
-                            ax = fmaf(q.x, wt, ax);
-                            ay = fmaf(q.y, wt, ay);
-                            az = fmaf(q.z, wt, az);
+                            ax = fmaf(dx, wt, ax);
+                            ay = fmaf(dy, wt, ay);
+                            az = fmaf(dz, wt, az);
                         }
                     } else {
                         if (d2 <= a.h2) {
@@ -289,13 +293,7 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
             }
         float phi;
         if (F == Field::kZB05) {
-            if (ws > 0.f) {
-                const float inv = 1.0f / ws;
-                const float ex = vx - ax * inv, ey = vy - ay * inv, ez = vz - az * inv;
-                phi = sqrtf(fmaf(ex, ex, fmaf(ey, ey, ez * ez))) - a.rp;
-            } else {
-                phi = 0.f;
-            }
+            phi = ws > 0.f ? sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az))) / ws - a.rp : 0.f;
         } else {
             phi = ws;
         }
@@ -620,8 +618,8 @@ __global__ void __launch_bounds__(kThreads) k_mc_classify(McArgs a, const Counte
             }
             if (all) {
                 uint32_t cs = 0;
-#pragma unroll
                 bool in_cap = true;
+#pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const uint32_t r = i == 0 ? t : (i == 4 ? t + 1 : band_rank(a.band, ids[i]));
                     // ranks beyond the capacity only occur in a frame that overflowed and is re-run
@@ -765,6 +763,7 @@ void launch_hash(const KernelCtx& c, const float* xyz, uint32_t n, const Grid& s
 {
     if (!n) return;
     k_hash<<<blocks_for(n), kThreads, 0, c.stream>>>(xyz, n, sp, keys, vals, ctr);
+    ++g_launches;
 }
 
 void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint32_t* perm, uint32_t n,
@@ -772,12 +771,14 @@ void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint3
 {
     if (!n) return;
     k_ranges_gather<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, perm, n, xyz, dens, sorted, ranges, occ);
+    ++g_launches;
 }
 
 void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf)
 {
     const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
     k_surface_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf);
+    ++g_launches;
 }
 
 void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, const uint8_t* surf,
@@ -785,6 +786,7 @@ void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* oc
 {
     const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
     k_involved_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf, invol);
+    ++g_launches;
 }
 
 void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges,
@@ -794,6 +796,7 @@ void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, con
     // -45 / (pi h^4) exactly as the reference evaluates it in double
     const double k = -45.0 / (3.1415926535 * (double)h2 * (double)h2);
     k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, h, k, mass, psurf);
+    ++g_launches;
 }
 
 void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t* skeys, const uint8_t* surf,
@@ -802,12 +805,14 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
 {
     if (!n) return;
     k_band_stamp<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc, thr, bits, ctr);
+    ++g_launches;
 }
 
 void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
                       uint32_t* sv, uint32_t cap, Counters* ctr)
 {
     k_band_list<<<persistent_blocks(c, nwords, 16), kThreads, 0, c.stream>>>(bits, prefix, nwords, sv, cap, ctr);
+    ++g_launches;
 }
 
 void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr)
@@ -815,6 +820,7 @@ void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counte
     const unsigned g = persistent_blocks(c, a.cap, 16);
     if (f == Field::kTC01) k_field_iso<Field::kTC01><<<g, kThreads, 0, c.stream>>>(a, ctr);
     else k_field_iso<Field::kZB05><<<g, kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
@@ -824,32 +830,38 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     // (1.0 - lambda) is evaluated in double and rounded (cu:656)
     const float oml = (float)(1.0 - (double)lambda);
     k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, oml, lambda, mass, mean, smoothed);
+    ++g_launches;
 }
 
 void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr)
 {
     if (!a.n) return;
     k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr)
 {
     k_field_aniso<<<persistent_blocks(c, a.cap, 16), kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr)
 {
     k_mc_classify<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_valid_list(const KernelCtx& c, const McArgs& a, Counters* ctr)
 {
     k_valid_list<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr)
 {
     k_mc_generate<<<persistent_blocks(c, a.cap_valid, 16), kThreads, 0, c.stream>>>(a, ctr);
+    ++g_launches;
 }
 
 void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint8_t* surf, const uint8_t* psurf,
@@ -857,6 +869,7 @@ void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint
 {
     if (!n) return;
     k_particle_flags<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, surf, psurf, n, out);
+    ++g_launches;
 }
 
 }  // namespace fsr

@@ -111,4 +111,8 @@ void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint
 
 void upload_mc_tables(cudaStream_t s);
 
+// Number of kernels launched by this thread through the wrappers (the
+// frame's gpu_launches figure).
+extern thread_local uint64_t g_launches;
+
 }  // namespace fsr

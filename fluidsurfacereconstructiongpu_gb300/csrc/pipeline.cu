@@ -256,6 +256,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         };
         if (timing) cudaEventRecord(h->ev_start, st);
 
+        const uint64_t launches0 = g_launches;
         CK(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
         CK(cudaMemsetAsync(h->ranges.ptr, 0xFF, 8ull * C, st));
         CK(cudaMemsetAsync(h->occ.ptr, 0, C, st));
@@ -419,6 +420,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         s.n_valid_cubes = hc.n_valid;
         s.n_mesh_vertices = hc.n_mesh_verts;
         s.n_fp64_fallbacks = hc.n_fp64;
+        s.n_kernel_launches = (uint32_t)(g_launches - launches0);
         for (int a = 0; a < 3; ++a) {
             s.spatial_res[a] = sp.res[a];
             s.scalar_res[a] = sc.res[a];

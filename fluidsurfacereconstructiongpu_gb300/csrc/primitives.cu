@@ -1,6 +1,7 @@
 // Exclusive scan (reduce-then-scan over 4096-element tiles) and stable LSD
 // radix sort (8-bit digits, per-warp match-based ranking).
 #include "primitives.h"
+#include "kernels.h"
 
 #include <algorithm>
 
@@ -146,6 +147,7 @@ void launch_scan(uint32_t g, const uint32_t* in, uint32_t* out, uint32_t n_host,
     k_tile_reduce<M><<<g, kScanThreads, 0, stream>>>(in, n_host, n_dev, n_max, scratch);
     k_scan_tile_sums<<<1, kScanThreads, 0, stream>>>(scratch, n_host, n_dev, n_max, total);
     k_tile_scan<M><<<g, kScanThreads, 0, stream>>>(in, out, n_host, n_dev, n_max, scratch);
+    g_launches += 3;
 }
 
 uint32_t grid_for_tiles(uint64_t n_max)
@@ -295,6 +297,7 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uin
         cudaError_t e = scan_u32(hist, hist, nhist, nullptr, nhist, nullptr, ScanInput::kValue, scan_tmp, stream);
         if (e != cudaSuccess) { *err = e; return cur; }
         k_radix_scatter<<<ntiles, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, n, shift, ntiles, hist);
+        g_launches += 2;
         cur ^= 1;
     }
     *err = cudaGetLastError();

@@ -92,6 +92,7 @@ typedef struct fsr_stats {
     uint32_t scalar_res[3];
     uint32_t n_fp64_fallbacks;     /* Yu13: eigen-solves redone in FP64 */
     uint32_t n_retries;            /* frame re-runs after a capacity grow */
+    uint32_t n_kernel_launches;    /* kernels launched by the last frame (its final attempt) */
     float stage_ms[FSR_NUM_STAGES];/* with FSR_FLAG_STAGE_TIMING */
     float total_ms;
 } fsr_stats;

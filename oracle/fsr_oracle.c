@@ -902,9 +902,12 @@ static inline real_t lerp_fac_gpu(real_t a, real_t b, real_t iso)
     return (iso - a) / d;
 }
 
-int o_generate(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32_t nq,
-               const o_gridinfo* sc, const uint32_t* nvScan, const real_t* phi, const o_simparam* p,
-               real_t* outPos, real_t* outNrm, uint64_t nOut)
+/* o_generate plus, per mesh vertex, the length of the interpolated normal
+ * before its normalisation (outLen, may be NULL): directions of short
+ * interpolated normals are ill-conditioned, which the tests account for. */
+int o_generate2(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32_t nq,
+                const o_gridinfo* sc, const uint32_t* nvScan, const real_t* phi, const o_simparam* p,
+                real_t* outPos, real_t* outNrm, real_t* outLen, uint64_t nOut)
 {
     (void)nb;
     const real_t iso = (real_t)p->isoValue;
@@ -929,7 +932,7 @@ int o_generate(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32
             normalize_gpu(cn[i]);
         }
         uint32_t ef = fsr_o_edge_flags(f), nv = fsr_o_num_vertices(f);
-        real_t ip[12][3], in[12][3];
+        real_t ip[12][3], in[12][3], il[12];
         for (int e = 0; e < 12; ++e) {
             if (!(ef & (1u << e))) continue;
             int a = FSR_O_EDGE[e][0], b = FSR_O_EDGE[e][1];
@@ -938,6 +941,7 @@ int o_generate(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32
                 ip[e][k] = cp[a][k] + t * (cp[b][k] - cp[a][k]);
                 in[e][k] = cn[a][k] + t * (cn[b][k] - cn[a][k]);
             }
+            il[e] = sqrt((double)(in[e][0] * in[e][0] + in[e][1] * in[e][1] + in[e][2] * in[e][2]));
             normalize_gpu(in[e]);
             for (int k = 0; k < 3; ++k) in[e][k] = sgn * in[e][k];
         }
@@ -949,9 +953,17 @@ int o_generate(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32
                 outPos[3 * (base + k) + j] = ip[e][j];
                 outNrm[3 * (base + k) + j] = in[e][j];
             }
+            if (outLen) outLen[base + k] = il[e];
         }
     }
     return bad ? ERR_ARG : OK;
+}
+
+int o_generate(const uint32_t* sv, uint32_t nb, const uint32_t* validIdx, uint32_t nq,
+               const o_gridinfo* sc, const uint32_t* nvScan, const real_t* phi, const o_simparam* p,
+               real_t* outPos, real_t* outNrm, uint64_t nOut)
+{
+    return o_generate2(sv, nb, validIdx, nq, sc, nvScan, phi, p, outPos, outNrm, NULL, nOut);
 }
 
 /* ------------------------------------------------------------------ */
@@ -970,8 +982,8 @@ static inline void normalize_host(real_t* n) /* fVector3::normalize, MathVector.
     }
 }
 
-int64_t o_mc_cpu(const real_t* phi, const o_gridinfo* sc, float iso_f, const uint32_t* cubeVertex,
-                 uint32_t nq, real_t* outPos, real_t* outNrm, uint64_t capacity)
+int64_t o_mc_cpu2(const real_t* phi, const o_gridinfo* sc, float iso_f, const uint32_t* cubeVertex,
+                  uint32_t nq, real_t* outPos, real_t* outNrm, real_t* outLen, uint64_t capacity)
 {
     const uint32_t* r = sc->res;
     const real_t iso = (real_t)iso_f;
@@ -994,7 +1006,7 @@ int64_t o_mc_cpu(const real_t* phi, const o_gridinfo* sc, float iso_f, const uin
         }
         if (f == 0 || f == 255) continue;
         uint32_t ef = fsr_o_edge_flags(f), nv = fsr_o_num_vertices(f);
-        real_t ip[12][3], in[12][3];
+        real_t ip[12][3], in[12][3], il[12];
         for (int e = 0; e < 12; ++e) {
             if (!(ef & (1u << e))) continue;
             int a = FSR_O_EDGE[e][0], b = FSR_O_EDGE[e][1];
@@ -1004,6 +1016,7 @@ int64_t o_mc_cpu(const real_t* phi, const o_gridinfo* sc, float iso_f, const uin
                 ip[e][k] = cp[a][k] + (cp[b][k] - cp[a][k]) * t;
                 in[e][k] = cn[a][k] + (cn[b][k] - cn[a][k]) * t;
             }
+            il[e] = sqrt((double)(in[e][0] * in[e][0] + in[e][1] * in[e][1] + in[e][2] * in[e][2]));
             normalize_host(in[e]);
         }
         if (out + nv > capacity) return -1;
@@ -1013,8 +1026,15 @@ int64_t o_mc_cpu(const real_t* phi, const o_gridinfo* sc, float iso_f, const uin
                 outPos[3 * (out + k) + j] = ip[e][j];
                 outNrm[3 * (out + k) + j] = in[e][j];
             }
+            if (outLen) outLen[out + k] = il[e];
         }
         out += nv;
     }
     return (int64_t)out;
+}
+
+int64_t o_mc_cpu(const real_t* phi, const o_gridinfo* sc, float iso_f, const uint32_t* cubeVertex,
+                 uint32_t nq, real_t* outPos, real_t* outNrm, uint64_t capacity)
+{
+    return o_mc_cpu2(phi, sc, iso_f, cubeVertex, nq, outPos, outNrm, NULL, capacity);
 }

@@ -161,6 +161,8 @@ def load(kind: str):
         raise FileNotFoundError(f"{kind} stage library not built: {path}")
     lib = ctypes.CDLL(path)
     lib.o_mc_cpu.restype = ctypes.c_int64
+    if hasattr(lib, "o_mc_cpu2"):
+        lib.o_mc_cpu2.restype = ctypes.c_int64
     _LIBS[kind] = lib
     return lib
 
@@ -246,10 +248,37 @@ class Frame:
         return 0 if self.mesh_pos is None else self.mesh_pos.shape[0] // 3
 
 
+class _TimedLib:
+    """Wraps a stage library and accumulates wall time per o_* call."""
+
+    def __init__(self, lib, times: dict):
+        self._lib, self._t = lib, times
+
+    def __getattr__(self, name):
+        f = getattr(self._lib, name)
+        if not name.startswith("o_") or name in ("o_real_bytes", "o_is_reference"):
+            return f
+
+        def call(*a):
+            import time
+            t0 = time.perf_counter()
+            r = f(*a)
+            self._t[name] = self._t.get(name, 0.0) + time.perf_counter() - t0
+            return r
+        return call
+
+
 def run_frame(kind: str, pos_in: np.ndarray, dens_in: np.ndarray, bbmin, bbmax,
-              params: FrameParams) -> Frame:
-    """Runs one frame of ``params.method`` with stage library ``kind``."""
+              params: FrameParams, times: Optional[dict] = None, field_stride: int = 1) -> Frame:
+    """Runs one frame of ``params.method`` with stage library ``kind``.
+
+    times: if given, receives the wall seconds spent in each stage library
+    call.  field_stride > 1 evaluates the field only at every field_stride-th
+    band vertex (a bounded timing sample: the field call's time is then
+    scaled by the sampling factor and the mesh is not meaningful)."""
     lib = load(kind)
+    if times is not None:
+        lib = _TimedLib(lib, times)
     real = np.float64 if lib.o_real_bytes() == 8 else np.float32
     is_ref = bool(lib.o_is_reference())
     iso, ratio, scale, _ = params.resolved()
@@ -328,22 +357,43 @@ def run_frame(kind: str, pos_in: np.ndarray, dens_in: np.ndarray, bbmin, bbmax,
                        ctypes.c_uint32(n), _ptr(ranges), _ptr(inv), ctypes.c_uint32(ni), _ptr(G))
         G = G[:ni]
         phi = np.full(V, YU13_FILL_BITS, dtype=np.uint32).view(np.float32).astype(real)
-        lib.o_field_aniso(ctypes.byref(prm), ctypes.c_uint32(nb), ctypes.byref(sc), ctypes.byref(sp),
+        svf = np.ascontiguousarray(sv[::field_stride]) if field_stride > 1 else sv
+        t_before = times.get("o_field_aniso", 0.0) if times is not None else 0.0
+        lib.o_field_aniso(ctypes.byref(prm), ctypes.c_uint32(svf.size), ctypes.byref(sc), ctypes.byref(sp),
                           _ptr(np.ascontiguousarray(G) if ni else np.zeros((1, 9), dtype=real)),
                           ctypes.c_uint32(ni), _ptr(smoothed), _ptr(dens), ctypes.c_uint32(n),
-                          _ptr(ranges), _ptr(sv), _ptr(ninv), _ptr(ninv_scan), _ptr(phi))
+                          _ptr(ranges), _ptr(svf), _ptr(ninv), _ptr(ninv_scan), _ptr(phi))
+        if times is not None and svf.size:
+            dt = times["o_field_aniso"] - t_before
+            times["o_field_aniso"] = t_before + dt * nb / svf.size
+            times["_unsampled_extra"] = times.get("_unsampled_extra", 0.0) + dt * (nb / svf.size - 1.0)
         fr.mean, fr.mean32, fr.smoothed, fr.inv, fr.G = mean, mean32, smoothed, inv, G
         fr.extra["ninv_scan"] = ninv_scan
     else:
         phi = np.zeros(V, dtype=real)
-        fn = lib.o_field_tc01 if params.method == "tc01" else lib.o_field_zb05
-        fn(_ptr(sv), ctypes.c_uint32(nb), _ptr(ranges), _ptr(pos), ctypes.c_uint32(n),
-           ctypes.byref(sp), ctypes.byref(sc), ctypes.byref(prm), _ptr(phi))
+        name = "o_field_tc01" if params.method == "tc01" else "o_field_zb05"
+        svf = np.ascontiguousarray(sv[::field_stride]) if field_stride > 1 else sv
+        t_before = times.get(name, 0.0) if times is not None else 0.0
+        getattr(lib, name)(_ptr(svf), ctypes.c_uint32(svf.size), _ptr(ranges), _ptr(pos), ctypes.c_uint32(n),
+                           ctypes.byref(sp), ctypes.byref(sc), ctypes.byref(prm), _ptr(phi))
+        if times is not None and svf.size:
+            dt = times[name] - t_before
+            times[name] = t_before + dt * nb / svf.size
+            times["_unsampled_extra"] = times.get("_unsampled_extra", 0.0) + dt * (nb / svf.size - 1.0)
     fr.phi = phi
 
     # --- marching cubes
+    _marching_cubes(lib, fr, phi, real)
+    return fr
+
+
+def _marching_cubes(lib, fr: Frame, phi: np.ndarray, real, with_lengths: bool = False) -> None:
+    """Marching-cubes stages on the frame's band and the given dense field
+    (ReconstructorGPUOurs.cpp:164-265; Akinci12.cpp:213-288)."""
+    sv, is_surf, prm, sc = fr.sv, fr.is_surf, fr.simparam, fr.scalar
+    nb = sv.size
     valid = np.zeros(nb, dtype=np.uint32)
-    if params.method == "akinci":
+    if fr.method == "akinci":
         lib.o_classify_akinci(_ptr(sv), ctypes.c_uint32(nb), _ptr(phi), ctypes.byref(sc),
                               _ptr(is_surf), ctypes.byref(prm), _ptr(valid))
         valid_idx = np.flatnonzero(valid == 1).astype(np.uint32)
@@ -351,14 +401,21 @@ def run_frame(kind: str, pos_in: np.ndarray, dens_in: np.ndarray, bbmin, bbmax,
         cap = 15 * valid_idx.size
         mp = np.zeros((max(cap, 1), 3), dtype=real)
         mn = np.zeros((max(cap, 1), 3), dtype=real)
-        cnt = lib.o_mc_cpu(_ptr(phi), ctypes.byref(sc), ctypes.c_float(prm.isoValue), _ptr(cube_vertex),
-                           ctypes.c_uint32(valid_idx.size), _ptr(mp), _ptr(mn), ctypes.c_uint64(cap))
+        if with_lengths:
+            ln = np.zeros(max(cap, 1), dtype=real)
+            cnt = lib.o_mc_cpu2(_ptr(phi), ctypes.byref(sc), ctypes.c_float(prm.isoValue), _ptr(cube_vertex),
+                                ctypes.c_uint32(valid_idx.size), _ptr(mp), _ptr(mn), _ptr(ln),
+                                ctypes.c_uint64(cap))
+        else:
+            cnt = lib.o_mc_cpu(_ptr(phi), ctypes.byref(sc), ctypes.c_float(prm.isoValue), _ptr(cube_vertex),
+                               ctypes.c_uint32(valid_idx.size), _ptr(mp), _ptr(mn), ctypes.c_uint64(cap))
         if cnt < 0:
             raise RuntimeError("host marching cubes overflow")
         fr.valid, fr.valid_idx = valid, valid_idx
         fr.mesh_pos, fr.mesh_nrm = mp[:cnt], mn[:cnt]
-        return fr
-
+        if with_lengths:
+            fr.extra["normal_len"] = ln[:cnt]
+        return
     nverts = np.zeros(nb, dtype=np.uint32)
     lib.o_classify(_ptr(sv), ctypes.c_uint32(nb), _ptr(phi), ctypes.byref(sc), _ptr(is_surf),
                    ctypes.byref(prm), _ptr(valid), _ptr(nverts))
@@ -366,12 +423,36 @@ def run_frame(kind: str, pos_in: np.ndarray, dens_in: np.ndarray, bbmin, bbmax,
     nv_scan, total = exclusive_scan(nverts)
     mp = np.zeros((max(total, 1), 3), dtype=real)
     mn = np.zeros((max(total, 1), 3), dtype=real)
-    lib.o_generate(_ptr(sv), ctypes.c_uint32(nb), _ptr(valid_idx), ctypes.c_uint32(valid_idx.size),
-                   ctypes.byref(sc), _ptr(nv_scan), _ptr(phi), ctypes.byref(prm), _ptr(mp), _ptr(mn),
-                   ctypes.c_uint64(total))
+    if with_lengths:
+        ln = np.zeros(max(total, 1), dtype=real)
+        lib.o_generate2(_ptr(sv), ctypes.c_uint32(nb), _ptr(valid_idx), ctypes.c_uint32(valid_idx.size),
+                        ctypes.byref(sc), _ptr(nv_scan), _ptr(phi), ctypes.byref(prm), _ptr(mp), _ptr(mn),
+                        _ptr(ln), ctypes.c_uint64(total))
+        fr.extra["normal_len"] = ln[:total]
+    else:
+        lib.o_generate(_ptr(sv), ctypes.c_uint32(nb), _ptr(valid_idx), ctypes.c_uint32(valid_idx.size),
+                       ctypes.byref(sc), _ptr(nv_scan), _ptr(phi), ctypes.byref(prm), _ptr(mp), _ptr(mn),
+                       ctypes.c_uint64(total))
     fr.valid, fr.nverts, fr.valid_idx, fr.nv_scan = valid, nverts, valid_idx, nv_scan
     fr.mesh_pos, fr.mesh_nrm = mp[:total], mn[:total]
-    return fr
+
+
+def marching_cubes_on(kind: str, fr: Frame, band_values: np.ndarray) -> Frame:
+    """Re-runs only the marching-cubes stages of a frame with library `kind`
+    on a field given at the frame's band vertices (e.g. a GPU's field); the
+    rest of the grid keeps the method's fill value.  Returns a new Frame
+    sharing the frame's inputs."""
+    lib = load(kind)
+    real = np.float64 if lib.o_real_bytes() == 8 else np.float32
+    if fr.method == "yu13":
+        phi = np.full(fr.scalar.count, YU13_FILL_BITS, dtype=np.uint32).view(np.float32).astype(real)
+    else:
+        phi = np.zeros(fr.scalar.count, dtype=real)
+    phi[fr.sv] = np.asarray(band_values, dtype=np.float32).astype(real)
+    out = Frame(method=fr.method, spatial=fr.spatial, scalar=fr.scalar, simparam=fr.simparam)
+    out.sv, out.is_surf, out.phi = fr.sv, fr.is_surf, phi
+    _marching_cubes(lib, out, phi, real, with_lengths=True)
+    return out
 
 
 def cube_cases(kind: str, fr: Frame, cubes: np.ndarray) -> np.ndarray:
