@@ -158,6 +158,43 @@ typedef enum fsr_debug_array {
 fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes,
                            uint64_t* bytes_needed);
 
+/* ---- spatial hashing without allocation ------------------------------
+ *
+ * No counterpart in the reference (its launchSpatialGridBuilding,
+ * ReconstructionCUDA.cu:1437-1481, cudaMallocs a key array on every call).
+ *
+ * For callers that must not allocate device memory: an application whose
+ * memory is owned by its own pool or arena, a simulation step that runs
+ * where a cudaMalloc (and the device-wide synchronisation it can cause) is
+ * not allowed, or a host that has reserved the device memory up front.
+ * The call hashes the particles into the spatial grid of `hdr` (cell size
+ * kernel_radius * cell_size_scale over the bounding box grown by one cell,
+ * as fsr_reconstruct does), sorts them stably by cell and writes:
+ *   d_sorted_xyz     N x 3 floats, particles in cell order
+ *   d_sorted_density N floats in the same order
+ *   d_cell_ranges    {start, end} per cell, 0xFFFFFFFF for empty cells;
+ *                    cell_capacity is the number of cells the buffer holds
+ *   d_perm           (optional) input index of each sorted particle
+ *   d_out_of_grid    (optional) device word: number of particles outside the
+ *                    grid (their results are meaningless when it is non-zero)
+ *   *n_cells         number of cells of the grid (host)
+ * Its scratch lives in a static device array sized for
+ * FSR_NOALLOC_MAX_PARTICLES particles (about 4.3 MB), which every process
+ * that loads the library holds on each device it uses until it exits; larger
+ * n is rejected with FSR_ERR_TOO_LARGE before any GPU work.  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  All calls on a device
+ * share the array: calls whose GPU work overlaps (two streams, two host
+ * threads) race and corrupt each other's results.  It calls no cudaMalloc or
+ * cudaFree; the work is queued on `stream` and nothing is synchronised. */
+#define FSR_NOALLOC_MAX_PARTICLES (1u << 18)
+
+fsr_status fsr_spatial_hash_noalloc(const fsr_frame_header* hdr, float cell_size_scale,
+                                    const float* d_xyz, const float* d_density, uint32_t n,
+                                    float* d_sorted_xyz, float* d_sorted_density,
+                                    uint32_t* d_cell_ranges, uint64_t cell_capacity, uint32_t* d_perm,
+                                    uint32_t* d_out_of_grid, uint64_t* n_cells, void* stream);
+
 /* ---- file formats -------------------------------------------------- */
 
 /* Parses an .xyz file (data_format.txt; ReconstructorGPU.cpp:200-290).
