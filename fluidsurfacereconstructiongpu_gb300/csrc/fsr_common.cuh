@@ -61,7 +61,7 @@ struct McConst {
 };
 
 #if defined(__CUDACC__)
-__device__ __forceinline__ uint32_t lin3(uint32_t x, uint32_t y, uint32_t z, const Grid& g)
+__device__ __forceinline__ uint32_t lin3(uint32_t x, uint32_t y, uint32_t z, const Grid g)
 {
     return z * g.res[0] * g.res[1] + y * g.res[0] + x;
 }
@@ -96,22 +96,43 @@ __device__ __forceinline__ float dot3_rn(float x, float y, float z)
     return __fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z));
 }
 
-// Cells c-ext .. c+ext clamped to the grid.
+// Cells c-ext .. c+ext clamped to the grid (scalar members: no local arrays).
 struct Window {
     int lo[3], hi[3];
 };
 
-__device__ __forceinline__ Window window(int cx, int cy, int cz, int ext, const Grid& g)
+__device__ __forceinline__ Window window(int cx, int cy, int cz, int ext, const Grid g)
 {
     Window w;
-    const int c[3] = {cx, cy, cz};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        w.lo[a] = clampi(c[a] - ext, 0, (int)g.res[a] - 1);
-        w.hi[a] = clampi(c[a] + ext, 0, (int)g.res[a] - 1);
-    }
+    w.lo[0] = clampi(cx - ext, 0, (int)g.res[0] - 1);
+    w.lo[1] = clampi(cy - ext, 0, (int)g.res[1] - 1);
+    w.lo[2] = clampi(cz - ext, 0, (int)g.res[2] - 1);
+    w.hi[0] = clampi(cx + ext, 0, (int)g.res[0] - 1);
+    w.hi[1] = clampi(cy + ext, 0, (int)g.res[1] - 1);
+    w.hi[2] = clampi(cz + ext, 0, (int)g.res[2] - 1);
     return w;
 }
+
+// Narrows a window to the cells whose extent on each axis comes within r of
+// point p.  Callers pass r with a relative margin, so every particle a
+// skipped cell holds lies farther than the unmargined radius on some axis
+// even after the roundings of its cell index and of the distance: terms that
+// contribute exactly zero are the only ones skipped.
+__device__ __forceinline__ Window narrow(const Window& w, float px, float py, float pz, float r, const Grid g)
+{
+    Window o;
+    const float inv = 1.0f / g.cs;
+    o.lo[0] = max(w.lo[0], __float2int_rd((px - r - g.min[0]) * inv));
+    o.lo[1] = max(w.lo[1], __float2int_rd((py - r - g.min[1]) * inv));
+    o.lo[2] = max(w.lo[2], __float2int_rd((pz - r - g.min[2]) * inv));
+    o.hi[0] = min(w.hi[0], __float2int_rd((px + r - g.min[0]) * inv));
+    o.hi[1] = min(w.hi[1], __float2int_rd((py + r - g.min[1]) * inv));
+    o.hi[2] = min(w.hi[2], __float2int_rd((pz + r - g.min[2]) * inv));
+    return o;
+}
+
+// Margin applied to culling radii: relative 1e-4 plus 1e-4 of a cell.
+__device__ __forceinline__ float cull_radius(float r, float cs) { return r * 1.0001f + 1e-4f * cs; }
 
 __device__ __forceinline__ bool band_has(const BandView& b, uint32_t v)
 {

@@ -44,7 +44,7 @@ struct fsr_handle {
     fsr::DevBuf mean, smoothed, grec;    // Yu13
     fsr::DevBuf pflags;                  // u32 surface flags (debug)
     // cell-sized
-    fsr::DevBuf ranges, occ, surf, invol;
+    fsr::DevBuf ranges, occ, surf, invol, cell_rmax;
     // vertex-sized
     fsr::DevBuf bits, prefix, scan_tmp;
     // band-sized

@@ -252,8 +252,10 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
         unlin3(a.sv[t], a.sc, x, y, z);
         const float vx = vpos1(x, a.sc.min[0], a.sc.cs), vy = vpos1(y, a.sc.min[1], a.sc.cs),
                     vz = vpos1(z, a.sc.min[2], a.sc.cs);
-        const Window w = window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
-                                cell1(vz, a.sp.min[2], a.sp.cs), 1, a.sp);
+        // only particles within h contribute: narrow the +-1 window to h
+        const Window w = narrow(window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
+                                       cell1(vz, a.sp.min[2], a.sp.cs), 1, a.sp),
+                                vx, vy, vz, cull_radius(a.h, a.sp.cs), a.sp);
         float ws = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
         for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
             for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
@@ -313,8 +315,11 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const float4 p = sorted[t];
-    const Window w = window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
-                            cell1(p.z, sp.min[2], sp.cs), 2, sp);
+    // cells beyond R on some axis only hold zero-weight particles, whose +0
+    // terms leave the exact sums unchanged: skip them
+    const Window w = narrow(window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
+                                   cell1(p.z, sp.min[2], sp.cs), 2, sp),
+                            p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
     float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
     for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
         for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
@@ -446,7 +451,7 @@ __device__ float make_G(const T V[3][3], const T w[3], float h_inv, float G[9])
 // when the covariance's condition number exceeds 1e4.
 // Output record per particle: (x,y,z smoothed, r2max) (G row 0, coef)
 // (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
-__global__ void __launch_bounds__(kThreads) k_cov(CovArgs a, Counters* ctr)
+__global__ void k_cov(CovArgs a, Counters* ctr)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = t < a.n && a.invol[a.skeys[t]];
@@ -454,8 +459,12 @@ __global__ void __launch_bounds__(kThreads) k_cov(CovArgs a, Counters* ctr)
     if (!act) return;
     const float4 p = a.sorted[t];
     const float4 m = a.mean[t];
-    const Window w = window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
-                            cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp);
+    // the window is centred on the particle's cell (cu:710-716); only
+    // particles within R of the mean count or weigh, so cells beyond R of the
+    // mean on some axis are skipped
+    const Window w = narrow(window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
+                                   cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp),
+                            m.x, m.y, m.z, cull_radius(a.R, a.sp.cs), a.sp);
     Kahan c11, c22, c33, c12, c13, c23, wsum;
     uint32_t nn = 0;
     for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
@@ -523,6 +532,9 @@ __global__ void __launch_bounds__(kThreads) k_cov(CovArgs a, Counters* ctr)
                       G[1] * G[3] * G[8] - G[2] * G[4] * G[6];
     const float4 sm = a.smoothed[t];
     const float r2 = rmax * rmax * 1.0001f;
+    // the cell's largest support radius, for the field's cell culling
+    // (positive floats order like their bit patterns)
+    atomicMax(reinterpret_cast<int*>(a.cell_rmax) + a.skeys[t], __float_as_int(rmax));
     float4* rec = a.grec + 4ull * t;
     rec[0] = make_float4(sm.x, sm.y, sm.z, r2);
     rec[1] = make_float4(G[0], G[1], G[2], a.sigma * det * sm.w);
@@ -533,7 +545,7 @@ __global__ void __launch_bounds__(kThreads) k_cov(CovArgs a, Counters* ctr)
 // computationOfScalarFieldGrid (cu:830-906): +-2 cell window; particles of
 // involved cells use sigma det(G) (1 - |G r|^2)^3, all other particles the
 // unscaled sigma (1 - |r|^2)^3 (cuh:312-322), each times m / rho.
-__global__ void __launch_bounds__(kThreads) k_field_aniso(AnisoFieldArgs a, const Counters* ctr)
+__global__ void k_field_aniso(AnisoFieldArgs a, const Counters* ctr)
 {
     const uint32_t nb = min(ctr->n_band, a.cap);
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
@@ -544,13 +556,25 @@ __global__ void __launch_bounds__(kThreads) k_field_aniso(AnisoFieldArgs a, cons
         const Window w = window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
                                 cell1(vz, a.sp.min[2], a.sp.cs), 2, a.sp);
         float sum = 0.f;
-        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy)
+        const float cs = a.sp.cs;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz) {
+            const float bz0 = a.sp.min[2] + zz * cs;
+            const float gz = fmaxf(0.f, fmaxf(bz0 - vz, vz - (bz0 + cs)));
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                const float by0 = a.sp.min[1] + yy * cs;
+                const float gy = fmaxf(0.f, fmaxf(by0 - vy, vy - (by0 + cs)));
+                const float gyz = fmaf(gy, gy, gz * gz);
                 for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx) {
                     const uint32_t c = lin3(xx, yy, zz, a.sp);
                     const uint2 r = __ldg(&a.ranges[c]);
                     if (r.x == kEmpty) continue;
                     if (__ldg(&a.invol[c])) {
+                        // skip the cell when the vertex lies beyond the largest
+                        // support radius of its particles: all terms are zero
+                        const float bx0 = a.sp.min[0] + xx * cs;
+                        const float gx = fmaxf(0.f, fmaxf(bx0 - vx, vx - (bx0 + cs)));
+                        const float cr = cull_radius(__ldg(&a.cell_rmax[c]), cs);
+                        if (fmaf(gx, gx, gyz) >= cr * cr) continue;
                         for (uint32_t i = r.x; i < r.y; ++i) {
                             const float4 r0 = __ldg(&a.grec[4ull * i]);
                             const float rx = r0.x - vx, ry = r0.y - vy, rz = r0.z - vz;
@@ -580,6 +604,8 @@ __global__ void __launch_bounds__(kThreads) k_field_aniso(AnisoFieldArgs a, cons
                         }
                     }
                 }
+            }
+        }
         a.phi[t] = sum - 0.5f;
     }
 }
@@ -598,7 +624,7 @@ __device__ __forceinline__ float field_at(const McArgs& a, int x, int y, int z)
 
 // detectValidSurfaceCubes (cu:328-364): a band vertex as cube origin is
 // valid when all 8 corners are band vertices and the case emits triangles.
-__global__ void __launch_bounds__(kThreads) k_mc_classify(McArgs a, const Counters* ctr)
+__global__ void k_mc_classify(McArgs a, const Counters* ctr)
 {
     const uint32_t nb = min(ctr->n_band, a.cap_band);
     const uint32_t rx = a.sc.res[0], rxy = a.sc.res[0] * a.sc.res[1];
@@ -680,7 +706,7 @@ __device__ __forceinline__ void normalize_guarded(float n[3])
 // generateTriangles (cu:383-463), or with host_mc the host marching cubes
 // of Akinci12 (MarchingCubesCPU.cpp:3-72: no normal sign flip, guarded
 // normalisation, epsilon test in double).
-__global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counters* ctr)
+__global__ void k_mc_generate(McArgs a, const Counters* ctr)
 {
     const uint32_t nq = min(ctr->n_valid, a.cap_valid);
     const uint32_t ntot = ctr->n_mesh_verts;

@@ -49,7 +49,7 @@ struct IsoFieldArgs {
     const uint2* ranges;
     const uint32_t* sv;
     float* phi;
-    float h2, inv_h2, rp;
+    float h, h2, inv_h2, rp;
     uint32_t cap;
 };
 void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr);
@@ -66,7 +66,8 @@ struct CovArgs {
     const uint2* ranges;
     const uint32_t* skeys;
     const uint8_t* invol;
-    float4* grec;  // 3 float4 per particle: G row-major, coef, r2max
+    float4* grec;  // 4 float4 per particle: (x,y,z smoothed, r2max) (G rows, coef in row 0's w)
+    float* cell_rmax;  // per cell: largest support radius of its particles (zeroed per frame)
     uint32_t n;
     float R, h, h2, h_inv, mass, sigma;
     uint32_t min_neighbors;
@@ -80,6 +81,7 @@ struct AnisoFieldArgs {
     const uint2* ranges;
     const uint8_t* invol;
     const uint8_t* occ;
+    const float* cell_rmax;
     const uint32_t* sv;
     float* phi;
     float sigma;

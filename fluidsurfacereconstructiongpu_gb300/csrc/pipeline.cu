@@ -172,7 +172,7 @@ fsr_handle::~fsr_handle()
 std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
-            &surf,   &invol,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
+            &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
             &qpos,   &valid,   &mean,   &smoothed, &grec, &mesh_pos, &mesh_nrm, &pflags, &ctr};
 }
 
@@ -221,6 +221,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
     CK(h->ctr.ensure(sizeof(Counters)));
     if (yu13) {
         CK(h->invol.ensure(C));
+        CK(h->cell_rmax.ensure(4ull * C));
         CK(h->mean.ensure(16ull * nn));
         CK(h->smoothed.ensure(16ull * nn));
         CK(h->grec.ensure(64ull * nn));
@@ -261,6 +262,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         CK(cudaMemsetAsync(h->ranges.ptr, 0xFF, 8ull * C, st));
         CK(cudaMemsetAsync(h->occ.ptr, 0, C, st));
         CK(cudaMemsetAsync(h->bits.ptr, 0, 4ull * nwords + 4, st));
+        if (yu13) CK(cudaMemsetAsync(h->cell_rmax.ptr, 0, 4ull * C, st));
 
         // ---- spatial hashing (ReconstructorGPU.cpp:292-313)
         uint32_t* k0 = (uint32_t*)h->keys0.ptr;
@@ -321,6 +323,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
             ca.skeys = skeys;
             ca.invol = (const uint8_t*)h->invol.ptr;
             ca.grec = (float4*)h->grec.ptr;
+            ca.cell_rmax = (float*)h->cell_rmax.ptr;
             ca.n = n;
             ca.R = R;
             ca.h = h_r;
@@ -339,6 +342,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
             fa.ranges = ranges;
             fa.invol = (const uint8_t*)h->invol.ptr;
             fa.occ = occ;
+            fa.cell_rmax = (const float*)h->cell_rmax.ptr;
             fa.sv = sv;
             fa.phi = phi;
             fa.sigma = ca.sigma;
@@ -354,6 +358,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
             fa.ranges = ranges;
             fa.sv = sv;
             fa.phi = phi;
+            fa.h = h_r;
             fa.h2 = h2;
             fa.inv_h2 = 1.0f / h2;
             fa.rp = hdr.particle_radius;
