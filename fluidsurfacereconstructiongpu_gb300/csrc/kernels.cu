@@ -1,6 +1,7 @@
 // Per-frame kernels of the reconstruction path.  Each kernel names the
 // reference kernel it replaces (ReconstructionCUDA.cu, "cu").
 #include "kernels.h"
+#include "cov_solver.cuh"
 
 #include <algorithm>
 
@@ -357,93 +358,6 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
                               __fdiv_rn(mass, p.w));
 }
 
-// Kahan-compensated FP32 accumulator.
-struct Kahan {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x)
-    {
-        const float y = x - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-};
-
-// Cyclic Jacobi eigen-decomposition of a symmetric 3x3 matrix (Golub & Van
-// Loan, Matrix Computations, sec. 8.5); columns of V are eigenvectors.
-template <class T>
-__device__ void sym_eig3(T A[3][3], T wv[3], T V[3][3])
-{
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? T(1) : T(0);
-    const T tol = sizeof(T) == 4 ? T(1e-14) : T(1e-30);
-    for (int sweep = 0; sweep < (sizeof(T) == 4 ? 12 : 24); ++sweep) {
-        const T off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
-        const T dia = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
-        if (!(off > tol * dia)) break;
-#pragma unroll
-        for (int pq = 0; pq < 3; ++pq) {
-            const int p = pq == 2 ? 1 : 0;
-            const int q = pq == 0 ? 1 : 2;
-            const T apq = A[p][q];
-            if (apq == T(0)) continue;
-            const T theta = (A[q][q] - A[p][p]) / (T(2) * apq);
-            const T sgn = theta >= T(0) ? T(1) : T(-1);
-            const T tt = sgn / (fabs(theta) + sqrt(theta * theta + T(1)));
-            const T cs = T(1) / sqrt(tt * tt + T(1));
-            const T sn = tt * cs;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const T akp = A[k][p], akq = A[k][q];
-                A[k][p] = cs * akp - sn * akq;
-                A[k][q] = sn * akp + cs * akq;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const T apk = A[p][k], aqk = A[q][k];
-                A[p][k] = cs * apk - sn * aqk;
-                A[q][k] = sn * apk + cs * aqk;
-            }
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const T vkp = V[k][p], vkq = V[k][q];
-                V[k][p] = cs * vkp - sn * vkq;
-                V[k][q] = sn * vkp + cs * vkq;
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) wv[i] = A[i][i];
-}
-
-// G = (1/h) cbrt(s1 s2 s3) V diag(1/s) V^T with s = |eigenvalues| clamped
-// from below at max(s)/4 (cu:790-822).  Returns the largest support radius
-// |r| with |G r| < 1, i.e. smax / cof.
-template <class T>
-__device__ float make_G(const T V[3][3], const T w[3], float h_inv, float G[9])
-{
-    T s0 = fabs(w[0]), s1 = fabs(w[1]), s2 = fabs(w[2]);
-    const T smax = fmax(s0, fmax(s1, s2));
-    const T lo = smax / T(4);
-    s0 = fmax(s0, lo);
-    s1 = fmax(s1, lo);
-    s2 = fmax(s2, lo);
-    const T cof = T(h_inv) * cbrt(s0 * s1 * s2);
-    const T inv[3] = {T(1) / s0, T(1) / s1, T(1) / s2};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            T acc = T(0);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) acc += V[i][k] * inv[k] * V[j][k];
-            G[3 * i + j] = (float)(acc * cof);
-        }
-    return (float)(smax / cof);
-}
-
 // calculationOfTransformMatricesForParticles (cu:689-827) for every
 // particle of an involved cell.  The neighbour count (dist <= r about the
 // FP32 mean, cu:746) is exact; the covariance is accumulated with Kahan
@@ -465,7 +379,7 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
     const Window w = narrow(window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
                                    cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp),
                             m.x, m.y, m.z, cull_radius(a.R, a.sp.cs), a.sp);
-    Kahan c11, c22, c33, c12, c13, c23, wsum;
+    CovAccum acc;
     uint32_t nn = 0;
     for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
         for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
@@ -483,58 +397,21 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
                 const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
                 const float d = __fsqrt_rn(dot3_rn(vx, vy, vz));
                 if (d <= a.R) ++nn;
-                if (d < a.R) {
-                    const float s = d / a.R;
-                    const float wt = 1.0f - s * s * s;
-                    wsum.add(wt);
-                    const float wx = wt * vx, wy = wt * vy;
-                    c11.add(wx * vx);
-                    c22.add(wy * vy);
-                    c33.add(wt * vz * vz);
-                    c12.add(wx * vy);
-                    c13.add(wx * vz);
-                    c23.add(wy * vz);
-                }
+                if (d < a.R) acc.add(vx, vy, vz, d, a.R);
             }
         }
     float G[9];
-    float rmax;
-    if (nn < a.min_neighbors) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) G[k] = 0.f;
-        G[0] = G[4] = G[8] = a.h_inv;
-        rmax = a.h;
-    } else {
-        const float iw = 1.0f / wsum.s;
-        // (h^2 I + sum) / wsum, the reference's seeded covariance (cu:718-723)
-        float A[3][3] = {{(a.h2 + c11.s) * iw, c12.s * iw, c13.s * iw},
-                         {c12.s * iw, (a.h2 + c22.s) * iw, c23.s * iw},
-                         {c13.s * iw, c23.s * iw, (a.h2 + c33.s) * iw}};
-        const float A0[3][3] = {{A[0][0], A[0][1], A[0][2]}, {A[1][0], A[1][1], A[1][2]}, {A[2][0], A[2][1], A[2][2]}};
-        float wv[3], V[3][3];
-        sym_eig3<float>(A, wv, V);
-        const float smax = fmaxf(fabsf(wv[0]), fmaxf(fabsf(wv[1]), fabsf(wv[2])));
-        const float smin = fminf(fabsf(wv[0]), fminf(fabsf(wv[1]), fabsf(wv[2])));
-        if (!(smin > 0.f) || smax > 1e4f * smin) {
-            double Ad[3][3], wd[3], Vd[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) Ad[i][j] = (double)A0[i][j];
-            sym_eig3<double>(Ad, wd, Vd);
-            rmax = make_G<double>(Vd, wd, a.h_inv, G);
-            atomicAdd(&ctr->n_fp64, 1u);
-        } else {
-            rmax = make_G<float>(V, wv, a.h_inv, G);
-        }
-    }
+    const float rmax = covariance_to_G(acc, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
     const float det = G[0] * G[4] * G[8] + G[1] * G[5] * G[6] + G[2] * G[3] * G[7] - G[0] * G[5] * G[7] -
                       G[1] * G[3] * G[8] - G[2] * G[4] * G[6];
     const float4 sm = a.smoothed[t];
     const float r2 = rmax * rmax * 1.0001f;
-    // the cell's largest support radius, for the field's cell culling
-    // (positive floats order like their bit patterns)
-    atomicMax(reinterpret_cast<int*>(a.cell_rmax) + a.skeys[t], __float_as_int(rmax));
+    // the cell's reach for the field's cell culling: support radius plus the
+    // smoothing displacement (the kernel sits at the smoothed position, which
+    // may lie outside the cell's box); positive floats order like their bits
+    const float dx = sm.x - p.x, dy = sm.y - p.y, dz = sm.z - p.z;
+    const float reach = rmax + sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz))) * 1.0001f;
+    atomicMax(reinterpret_cast<int*>(a.cell_rmax) + a.skeys[t], __float_as_int(reach));
     float4* rec = a.grec + 4ull * t;
     rec[0] = make_float4(sm.x, sm.y, sm.z, r2);
     rec[1] = make_float4(G[0], G[1], G[2], a.sigma * det * sm.w);
@@ -569,8 +446,9 @@ __global__ void k_field_aniso(AnisoFieldArgs a, const Counters* ctr)
                     const uint2 r = __ldg(&a.ranges[c]);
                     if (r.x == kEmpty) continue;
                     if (__ldg(&a.invol[c])) {
-                        // skip the cell when the vertex lies beyond the largest
-                        // support radius of its particles: all terms are zero
+                        // skip the cell when the vertex lies beyond the reach
+                        // (support + smoothing shift) of all its particles:
+                        // every term is zero
                         const float bx0 = a.sp.min[0] + xx * cs;
                         const float gx = fmaxf(0.f, fmaxf(bx0 - vx, vx - (bx0 + cs)));
                         const float cr = cull_radius(__ldg(&a.cell_rmax[c]), cs);

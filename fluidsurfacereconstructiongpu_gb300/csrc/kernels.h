@@ -67,7 +67,7 @@ struct CovArgs {
     const uint32_t* skeys;
     const uint8_t* invol;
     float4* grec;  // 4 float4 per particle: (x,y,z smoothed, r2max) (G rows, coef in row 0's w)
-    float* cell_rmax;  // per cell: largest support radius of its particles (zeroed per frame)
+    float* cell_rmax;  // per cell: largest support radius + smoothing shift of its particles (zeroed per frame)
     uint32_t n;
     float R, h, h2, h_inv, mass, sigma;
     uint32_t min_neighbors;
