@@ -88,6 +88,10 @@ struct AnisoFieldArgs {
     uint32_t cap;
 };
 void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr);
+// Window-grouped evaluation with shared-memory candidate staging; returns
+// false (nothing launched) when the grid ratio makes a group too large.
+bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& a, const BandView& band, uint32_t ratio,
+                                Counters* ctr);
 
 struct McArgs {
     Grid sc;

@@ -347,7 +347,8 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
             fa.phi = phi;
             fa.sigma = ca.sigma;
             fa.cap = h->cap_band;
-            launch_field_aniso(kc, fa, ctr);
+            if (!launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr))
+                launch_field_aniso(kc, fa, ctr);
         } else {
             mark(5);
             mark(6);
