@@ -79,6 +79,8 @@ def _load():
         "fsr_mesh_device": (ctypes.c_int, [c_vp, P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_copy_mesh": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, P(c_u64)]),
         "fsr_get_stats": (ctypes.c_int, [c_vp, P(Stats)]),
+        "fsr_copy_mesh_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, P(c_u64), c_vp]),
+        "fsr_backward": (ctypes.c_int, [c_vp, c_vp, c_vp, P(c_f32), c_vp]),
         "fsr_debug_fetch": (ctypes.c_int, [c_vp, c_u32, c_vp, c_u64, P(c_u64)]),
         "fsr_read_xyz": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_free_host": (None, [c_vp]),

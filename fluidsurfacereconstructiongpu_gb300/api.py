@@ -151,6 +151,34 @@ class Reconstructor:
         N.check(N.lib.fsr_copy_mesh(self._h, pos.ctypes.data, nrm.ctypes.data, nv, ctypes.byref(out)), self._h)
         return Mesh(pos[:nv], nrm[:nv])
 
+    def mesh_tensors(self, stream=None):
+        """The last frame's triangle soup as two (3T, 3) CUDA tensors (copies)."""
+        import torch
+        nv = int(self.stats().n_mesh_vertices)
+        pos = torch.empty((nv, 3), dtype=torch.float32, device="cuda")
+        nrm = torch.empty((nv, 3), dtype=torch.float32, device="cuda")
+        s = stream if stream is not None else torch.cuda.current_stream()
+        out = ctypes.c_uint64(0)
+        N.check(N.lib.fsr_copy_mesh_device(self._h, ctypes.c_void_p(pos.data_ptr()), ctypes.c_void_p(nrm.data_ptr()),
+                                           nv, ctypes.byref(out), ctypes.c_void_p(s.cuda_stream)), self._h)
+        return pos, nrm
+
+    def backward(self, grad_mesh_pos, stream=None, with_radius: bool = False):
+        """dL/d(particle positions) (N, 3) in input order from dL/d(mesh vertex
+        positions) (3T, 3) of the last frame; optionally also dL/d(particle
+        radius) (ZB05 / Akinci12)."""
+        import torch
+        n = int(self.stats().n_particles)
+        g = grad_mesh_pos.contiguous().to(torch.float32)
+        assert g.is_cuda and g.shape == (int(self.stats().n_mesh_vertices), 3)
+        out = torch.empty((n, 3), dtype=torch.float32, device=g.device)
+        s = stream if stream is not None else torch.cuda.current_stream(g.device)
+        rad = ctypes.c_float(0.0)
+        N.check(N.lib.fsr_backward(self._h, ctypes.c_void_p(g.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                   ctypes.byref(rad) if with_radius else None, ctypes.c_void_p(s.cuda_stream)),
+                self._h)
+        return (out, float(rad.value)) if with_radius else out
+
     def mesh_device_ptrs(self):
         p, q, nv = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
         N.check(N.lib.fsr_mesh_device(self._h, ctypes.byref(p), ctypes.byref(q), ctypes.byref(nv)), self._h)

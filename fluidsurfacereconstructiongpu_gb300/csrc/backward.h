@@ -1,0 +1,39 @@
+// Backward pass of a reconstructed frame (see backward.cu).
+#pragma once
+
+#include "kernels.h"
+
+namespace fsr {
+
+struct BwdArgs {
+    Grid sp, sc;
+    uint32_t ratio;
+    uint32_t n;
+    BandView band;
+    const uint32_t* sv;
+    const uint32_t* valid;
+    const uint32_t* mc;
+    const uint32_t* vofs;
+    const uint64_t* tri;     // packed marching-cubes triangle table (device)
+    const float* gmesh;      // dL/d mesh vertex positions, 3 floats each
+    float* gphi;             // dL/dphi per band vertex (zeroed)
+    uint8_t* gkey;           // per window-centre key: holds a vertex with dL/dphi != 0 (zeroed)
+    const float4* sorted;
+    const uint32_t* skeys;
+    const uint32_t* perm;
+    const uint8_t* invol;
+    const float4* smoothed;
+    const float4* grec;
+    const float4* mv;        // ZB05: per band vertex (mean - v, weight sum)
+    float4* gsmooth;         // dL/d smoothed position (Yu13)
+    float4* gG;              // dL/dG, 3 float4 rows per particle (Yu13)
+    float4* gmean;           // dL/d mean from the covariance (Yu13)
+    float4* gx;              // dL/dx in sorted order (zeroed)
+    float iso, h, sigma;
+    uint32_t cap_band, cap_valid;
+};
+
+void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, const Counters* ctr, int method,
+                     float lambda, float R, float* radius_grad_dev, float* out_grad_xyz);
+
+}  // namespace fsr

@@ -45,19 +45,6 @@ struct GroupArgs {
     uint32_t vlist_cap;             // capacity of the per-block vertex list
 };
 
-// First grid-vertex index along AXIS whose FP32 cell index is >= c (the
-// boundary lies within a vertex or two of c * ratio).
-template <int AXIS>
-__device__ __forceinline__ int first_vertex(int c, const Grid& sc, const Grid& sp, uint32_t ratio)
-{
-    int x = max(0, c * (int)ratio - 1);
-    const int nres = (int)sc.res[AXIS];
-    if (x > nres) x = nres;
-    while (x > 0 && cell1(vpos1(x - 1, sc.min[AXIS], sc.cs), sp.min[AXIS], sp.cs) >= c) --x;
-    while (x < nres && cell1(vpos1(x, sc.min[AXIS], sc.cs), sp.min[AXIS], sp.cs) < c) ++x;
-    return x;
-}
-
 __global__ void k_field_aniso_grouped(GroupArgs a, uint32_t ratio, const Counters* ctr)
 {
     extern __shared__ __align__(16) unsigned char smem[];

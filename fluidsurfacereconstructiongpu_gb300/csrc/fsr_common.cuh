@@ -145,6 +145,20 @@ __device__ __forceinline__ uint32_t band_rank(const BandView& b, uint32_t v)
     return __ldg(b.prefix + (v >> 5)) + __popc(w & ((1u << (v & 31u)) - 1u));
 }
 
+// First grid-vertex index along AXIS whose FP32 cell index (getIndex3D of
+// the vertex position) is >= c.  The cell index is non-decreasing along the
+// axis; the boundary lies within a vertex or two of c * ratio.
+template <int AXIS>
+__device__ __forceinline__ int first_vertex(int c, const Grid& sc, const Grid& sp, uint32_t ratio)
+{
+    int x = max(0, c * (int)ratio - 1);
+    const int nres = (int)sc.res[AXIS];
+    if (x > nres) x = nres;
+    while (x > 0 && cell1(vpos1(x - 1, sc.min[AXIS], sc.cs), sp.min[AXIS], sp.cs) >= c) --x;
+    while (x < nres && cell1(vpos1(x, sc.min[AXIS], sc.cs), sp.min[AXIS], sp.cs) < c) ++x;
+    return x;
+}
+
 #endif  // __CUDACC__
 
 }  // namespace fsr

@@ -52,6 +52,9 @@ struct fsr_handle {
     // mesh
     fsr::DevBuf mesh_pos, mesh_nrm;
     fsr::DevBuf ctr;
+    // backward pass
+    fsr::DevBuf mv;                      // ZB05/Akinci12: per band vertex (mean - v, weight sum)
+    fsr::DevBuf gphi, gkey, gsmooth, gG, gmean, gx, gscalar, tri;
 
     uint32_t cap_band = 0, cap_valid = 0, cap_mesh = 0;
     fsr::Counters* pinned_ctr = nullptr;
@@ -63,6 +66,7 @@ struct fsr_handle {
     fsr_stats stats{};
     fsr::Grid grid_sp{}, grid_sc{};
     uint64_t n_last = 0, C_last = 0, V_last = 0;
+    fsr_frame_header hdr_last{};
     const uint32_t* perm_ptr = nullptr;
     const uint32_t* skeys_ptr = nullptr;
 

@@ -297,6 +297,10 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
         float phi;
         if (F == Field::kZB05) {
             phi = ws > 0.f ? sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az))) / ws - a.rp : 0.f;
+            if (a.mv) {
+                const float inv = ws > 0.f ? 1.0f / ws : 0.f;
+                a.mv[t] = make_float4(ax * inv, ay * inv, az * inv, ws);
+            }
         } else {
             phi = ws;
         }

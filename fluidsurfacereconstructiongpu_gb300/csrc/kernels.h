@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include "fsr_common.cuh"
+#include "../../include/fsr.h"
 
 namespace fsr {
 
@@ -49,6 +50,7 @@ struct IsoFieldArgs {
     const uint2* ranges;
     const uint32_t* sv;
     float* phi;
+    float4* mv;  // optional (ZB05): per band vertex (mean - v, weight sum), kept for the backward pass
     float h, h2, inv_h2, rp;
     uint32_t cap;
 };

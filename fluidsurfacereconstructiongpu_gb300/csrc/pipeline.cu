@@ -173,7 +173,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &mesh_pos, &mesh_nrm, &pflags, &ctr};
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &mesh_pos, &mesh_nrm, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -251,6 +251,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         CK(h->valid.ensure(4ull * h->cap_valid));
         CK(h->mesh_pos.ensure(12ull * h->cap_mesh));
         CK(h->mesh_nrm.ensure(12ull * h->cap_mesh));
+        if (!yu13 && p.method != FSR_METHOD_TC01) CK(h->mv.ensure(16ull * h->cap_band));
 
         auto mark = [&](int stage) {
             if (timing) cudaEventRecord(h->ev[stage], st);
@@ -363,6 +364,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
             fa.h2 = h2;
             fa.inv_h2 = 1.0f / h2;
             fa.rp = hdr.particle_radius;
+            fa.mv = p.method == FSR_METHOD_TC01 ? nullptr : (float4*)h->mv.ptr;
             fa.cap = h->cap_band;
             launch_field_iso(kc, p.method == FSR_METHOD_TC01 ? Field::kTC01 : Field::kZB05, fa, ctr);
         }
@@ -447,6 +449,7 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         h->n_last = n;
         h->C_last = C;
         h->V_last = V;
+        h->hdr_last = hdr;
         return FSR_OK;
     }
     return fail(h, FSR_ERR_OUT_OF_MEMORY, "capacity growth did not converge");

@@ -136,6 +136,24 @@ fsr_status fsr_mesh_device(fsr_handle* h, const float** d_pos, const float** d_n
 fsr_status fsr_copy_mesh(fsr_handle* h, float* out_pos, float* out_nrm, uint64_t capacity,
                          uint64_t* n_vertices);
 
+/* Device-to-device copy of the last frame's mesh into caller buffers
+ * (either pointer may be NULL); queued on `stream`. */
+fsr_status fsr_copy_mesh_device(fsr_handle* h, float* d_pos, float* d_nrm, uint64_t capacity,
+                                uint64_t* n_vertices, void* stream);
+
+/* Backward pass of the last frame (no counterpart in the reference, which
+ * has no gradients).  Given dL/d(mesh vertex positions) of a scalar loss L
+ * (device, 3 floats per mesh vertex, the frame's triangle soup order), writes
+ * dL/d(particle positions) (device, N x 3 floats, the frame's input order) and,
+ * when grad_particle_radius is not NULL, dL/d(particle radius) (host scalar;
+ * ZB05 and Akinci12, 0 for the other fields).  The frame's discrete structure
+ * is held fixed: sorted order, band, valid cubes and cases, neighbourhoods and
+ * isolated-particle decisions; normals are not differentiated.  Neighbour
+ * sets are recomputed, not stored.  Queued on `stream`; synchronises it only
+ * to return the radius gradient. */
+fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, float* d_grad_xyz,
+                        float* grad_particle_radius, void* stream);
+
 fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out);
 
 /* Intermediates of the last frame (requires FSR_FLAG_KEEP_INTERMEDIATES for
