@@ -31,12 +31,15 @@ WORKLOADS = {
     # the anisotropic 1M frame (headline)
     "aniso1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="yu13", smoothing_lambda=0.9,
                     aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
+    # the anisotropic frame at 2^18 particles (profiling captures)
+    "aniso256k": dict(kind="dam_break", n=1 << 18, r=0.004, seed=2, method="yu13", smoothing_lambda=0.9,
+                      aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
     # the same frame with the plain ZB05 path (grid spacing 0.5r: ratio 8 at cell = h)
     "plain1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="zb05", grid_ratio=8),
     # 32^3 lattice, ZB05, grid spacing 0.5r
     "plain32k": dict(kind="lattice", n_side=32, r=0.0125, seed=1, method="zb05", grid_ratio=8),
 }
-METRIC = "particles/s recon (fwd) @1M aniso"
+METRIC = "particles/s recon (fwd, fwd+bwd) @1M aniso vs plain path; % HBM roofline"
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 
 
@@ -154,6 +157,81 @@ def committed_traffic(kernel_key):
     return d.get(kernel_key)
 
 
+BATCH = dict(frames=64, n_lo=20000, n_hi=400000, seed=3, methods=("akinci12", "zb05", "yu13"),
+             # grid spacing 0.5r everywhere (ratio 8 at cell = h); the anisotropic
+             # frames use the 1M anisotropic frame's settings
+             params={"akinci12": dict(grid_ratio=8), "zb05": dict(grid_ratio=8),
+                     "yu13": dict(smoothing_lambda=0.9, aniso_radius_over_h=1.0, cell_size_scale=1.25,
+                                  grid_ratio=10, iso=0.0)})
+
+
+def batch_frames(cfg=BATCH):
+    """64 frames, particle counts log-uniform in [20k, 400k], each the 32^3
+    lattice generator rescaled to its count, field drawn per frame."""
+    from fluidsurfacereconstructiongpu_gb300 import synthetic
+    rng = np.random.default_rng(cfg["seed"])
+    out = []
+    for i in range(cfg["frames"]):
+        n = int(np.exp(rng.uniform(np.log(cfg["n_lo"]), np.log(cfg["n_hi"]))))
+        m = cfg["methods"][int(rng.integers(len(cfg["methods"])))]
+        out.append((m, synthetic.lattice_count(n, seed=cfg["seed"] * 1000 + i)))
+    return out
+
+
+def run_batch_leg(dev, stream, steps, warmup, flush):
+    """The batched forward (one graph launch for all frames) against the
+    single-frame path on the same frames; both device-resident."""
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api
+    frames = batch_frames()
+    total = sum(fr.n for _, fr in frames)
+    args = [(m, torch.from_numpy(fr.pos).to(dev), torch.from_numpy(fr.density).to(dev), api.header_of(fr))
+            for m, fr in frames]
+    b = api.Batch(dev.index or 0, params=BATCH["params"])
+    b.reconstruct(args, stream=stream)  # plan + autotune
+    for _ in range(max(warmup - 1, 1)):
+        b.reconstruct(args, stream=stream)
+    torch.cuda.synchronize(dev)
+    ms_b = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.reconstruct(args, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms_b.append(e0.elapsed_time(e1))
+    tun = b.tuning()
+    launches = int(tun.kernels_per_launch)
+    b.close()
+    recs = {m: api.Reconstructor(m, dev.index or 0, **BATCH["params"][m]) for m in set(m for m, _ in frames)}
+    for _ in range(warmup):
+        for m, x, d, hdr in args:
+            recs[m].reconstruct(x, d, hdr, stream)
+    torch.cuda.synchronize(dev)
+    ms_s = []
+    for _ in range(steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for m, x, d, hdr in args:
+            recs[m].reconstruct(x, d, hdr, stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms_s.append(e0.elapsed_time(e1))
+    for r in recs.values():
+        r.close()
+    tb, ts = float(np.mean(ms_b)), float(np.mean(ms_s))
+    return {"frames": len(frames), "particles": total, "methods": {m: sum(1 for q, _ in frames if q == m)
+                                                                    for m in BATCH["methods"]},
+            "value": total / (tb / 1e3), "ms_per_step": tb, "single_frame_value": total / (ts / 1e3),
+            "single_frame_ms": ts, "speedup_vs_single_frame": ts / tb, "lanes": int(tun.lanes),
+            "grid_div": int(tun.grid_div), "autotune_candidates": int(tun.n_candidates),
+            "gpu_launches_per_step": launches,
+            "note": "step = one fsr_reconstruct_batch call (inputs copied device-to-device, one graph launch, "
+                    "one synchronisation); single frame = the same frames through fsr_reconstruct one by one"}
+
+
 def dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -202,6 +280,8 @@ def main():
     ap.add_argument("--cpu-field-stride", type=int, default=4,
                     help="CPU baseline: evaluate the field at every k-th band vertex and scale its time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-backward", action="store_true", help="skip the forward+backward leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames leg")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -265,6 +345,50 @@ def main():
         t_step = float(tt.item())
     value = fr.n * world / t_step
 
+    # forward + backward: the same frame, then dL/dx from a fixed dL/d(mesh) (the
+    # gradient of the mean squared distance of the mesh vertices to a sphere)
+    fb = None
+    if not args.no_backward:
+        mpos, _ = rec.mesh_tensors(stream)
+        c = mpos.mean(dim=0)
+        d = mpos - c
+        rr = d.norm(dim=1, keepdim=True).clamp_min(1e-12)
+        gmesh = (2.0 * (rr - rr.mean()) / rr / mpos.shape[0] * d).contiguous()
+        gx = torch.empty((fr.n, 3), dtype=torch.float32, device=dev)
+        import ctypes as _ct
+
+        def bwd():
+            _native.check(_native.lib.fsr_backward(rec._h, _ct.c_void_p(gmesh.data_ptr()), _ct.c_void_p(gx.data_ptr()),
+                                                   None, _ct.c_void_p(stream.cuda_stream)), rec._h)
+        for _ in range(args.warmup):
+            rec.reconstruct(xyz, den, hdr, stream)
+            bwd()
+        torch.cuda.synchronize(dev)
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            rec.reconstruct(xyz, den, hdr, stream)
+            ev[k][1].record(stream)
+            bwd()
+            ev[k][2].record(stream)
+        torch.cuda.synchronize(dev)
+        t_fb = float(np.mean([a.elapsed_time(c_) for a, _, c_ in ev])) / 1e3
+        t_b = float(np.mean([b.elapsed_time(c_) for _, b, c_ in ev])) / 1e3
+        if pg:
+            tt = torch.tensor([t_fb], dtype=torch.float64, device=dev)
+            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+            t_fb = float(tt.item())
+        n_bwd = int(rec.stats().n_backward_launches)
+        fb = {"value": fr.n * world / t_fb, "unit": "particles/s", "ms_per_step": t_fb * 1e3,
+              "backward_ms": t_b * 1e3, "backward_launches_per_step": n_bwd,
+              "loss": "mean over mesh vertices of (|v - c| - mean |v - c|)^2, c = mesh centroid (gradient fixed)"}
+        st = rec.stats()
+
+    batched = None
+    if not args.no_batch:
+        batched = run_batch_leg(dev, stream, args.steps, args.warmup, flush)
+
     # end to end through the host API: pinned inputs in, mesh out, every step
     pin_xyz = torch.from_numpy(fr.pos).pin_memory()
     pin_den = torch.from_numpy(fr.density).pin_memory()
@@ -312,7 +436,9 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": fr.n / e2e_step, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": (int(st.n_kernel_launches) * args.steps if hasattr(st, "n_kernel_launches") else None),
+            "fwd_bwd": fb,
+            "batched": batched,
+            "gpu_launches": int(st.n_kernel_launches) * args.steps,
             "stage_ms": {n: round(float(v), 4) for n, v in zip(_native.STAGE_NAMES, stage)},
             "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu}
     if rank == 0:

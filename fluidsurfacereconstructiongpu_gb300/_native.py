@@ -25,6 +25,7 @@ STATUS_NAMES = {
 METHOD_ZB05, METHOD_TC01, METHOD_YU13, METHOD_AKINCI12 = 0, 1, 2, 3
 FLAG_KEEP_INTERMEDIATES = 0x1
 FLAG_STAGE_TIMING = 0x2
+FLAG_SMALL_POOLS = 0x4
 
 DBG = dict(perm=0, sorted_xyz=1, ranges=2, surface_flags=3, involved_counts=4, band=5, field=6,
            mc_info=7, valid=8, mean=9, smoothed=10, G=11)
@@ -50,7 +51,7 @@ class Stats(ctypes.Structure):
                 ("n_surface_particles", c_u64), ("n_involved_particles", c_u64), ("n_band_vertices", c_u64),
                 ("n_valid_cubes", c_u64), ("n_mesh_vertices", c_u64), ("spatial_res", c_u32 * 3),
                 ("scalar_res", c_u32 * 3), ("n_fp64_fallbacks", c_u32), ("n_retries", c_u32),
-                ("n_kernel_launches", c_u32),
+                ("n_kernel_launches", c_u32), ("n_backward_launches", c_u32),
                 ("stage_ms", c_f32 * NUM_STAGES), ("total_ms", c_f32)]
 
 
@@ -58,6 +59,20 @@ class FsrError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
         self.status = status
+
+
+class BatchFrame(ctypes.Structure):
+    _fields_ = [("header", FrameHeader), ("method", c_u32), ("reserved", c_u32), ("n_particles", c_u64),
+                ("xyz", c_vp), ("density", c_vp)]
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("lanes", c_u32), ("grid_div", c_u32), ("n_candidates", c_u32), ("kernels_per_launch", c_u32),
+                ("graph_ms", c_f32), ("frames_ms", c_f32)]
+
+
+BATCH_RETUNE = 0x1
+BATCH_NO_AUTOTUNE = 0x2
 
 
 def _load():
@@ -81,6 +96,14 @@ def _load():
         "fsr_get_stats": (ctypes.c_int, [c_vp, P(Stats)]),
         "fsr_copy_mesh_device": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, P(c_u64), c_vp]),
         "fsr_backward": (ctypes.c_int, [c_vp, c_vp, c_vp, P(c_f32), c_vp]),
+        "fsr_batch_create": (ctypes.c_int, [c_vp, ctypes.c_int, P(c_vp)]),
+        "fsr_batch_destroy": (None, [c_vp]),
+        "fsr_batch_last_error": (ctypes.c_char_p, [c_vp]),
+        "fsr_reconstruct_batch": (ctypes.c_int, [c_vp, c_vp, c_u32, c_u32, c_vp]),
+        "fsr_batch_get_tuning": (ctypes.c_int, [c_vp, P(BatchTuning)]),
+        "fsr_batch_frame_stats": (ctypes.c_int, [c_vp, c_u32, P(Stats)]),
+        "fsr_batch_mesh_device": (ctypes.c_int, [c_vp, c_u32, P(c_vp), P(c_vp), P(c_u64)]),
+        "fsr_batch_copy_mesh": (ctypes.c_int, [c_vp, c_u32, c_vp, c_vp, c_u64, P(c_u64)]),
         "fsr_debug_fetch": (ctypes.c_int, [c_vp, c_u32, c_vp, c_u64, P(c_u64)]),
         "fsr_read_xyz": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_free_host": (None, [c_vp]),

@@ -206,6 +206,87 @@ class Reconstructor:
         return out
 
 
+class Batch:
+    """Many frames (mixed methods, uneven sizes) in one CUDA graph launch.
+
+    ``params`` maps method names to keyword overrides of that method's
+    defaults (the Reconstructor keywords iso, grid_ratio, cell_size_scale,
+    smoothing_lambda, aniso_radius_over_h, min_neighbors)."""
+
+    def __init__(self, device: int = 0, params: Optional[dict] = None):
+        arr = (N.Params * 4)()
+        for m in range(4):
+            N.check(N.lib.fsr_default_params(m, ctypes.byref(arr[m])))
+        for name, kw in (params or {}).items():
+            p = arr[METHODS[name]]
+            for k, v in kw.items():
+                setattr(p, "iso_value" if k == "iso" else k, v)
+        self._arr = arr
+        h = ctypes.c_void_p()
+        N.check(N.lib.fsr_batch_create(arr, int(device), ctypes.byref(h)))
+        self._b = h
+        self.count = 0
+
+    def close(self):
+        if getattr(self, "_b", None):
+            N.lib.fsr_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != N.FSR_OK:
+            raise N.FsrError(st, N.lib.fsr_batch_last_error(self._b).decode())
+
+    def reconstruct(self, frames, stream=None, retune: bool = False, autotune: bool = True):
+        """frames: list of (method, xyz (N,3) float32, density (N,), header);
+        xyz/density CUDA tensors or numpy arrays."""
+        import torch
+        arr = (N.BatchFrame * len(frames))()
+        keep = []
+        for i, (method, xyz, den, hdr) in enumerate(frames):
+            if isinstance(xyz, np.ndarray):
+                xyz = np.ascontiguousarray(xyz, np.float32)
+                den = np.ascontiguousarray(den, np.float32)
+                px, pd = xyz.ctypes.data, den.ctypes.data
+            else:
+                xyz = xyz.contiguous()
+                den = den.contiguous()
+                px, pd = xyz.data_ptr(), den.data_ptr()
+            keep.append((xyz, den))
+            arr[i].header = hdr
+            arr[i].method = METHODS[method]
+            arr[i].n_particles = int(den.shape[0])
+            arr[i].xyz = px
+            arr[i].density = pd
+        flags = (N.BATCH_RETUNE if retune else 0) | (0 if autotune else N.BATCH_NO_AUTOTUNE)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._check(N.lib.fsr_reconstruct_batch(self._b, arr, len(frames), flags, ctypes.c_void_p(s.cuda_stream)))
+        self.count = len(frames)
+
+    def tuning(self) -> N.BatchTuning:
+        t = N.BatchTuning()
+        self._check(N.lib.fsr_batch_get_tuning(self._b, ctypes.byref(t)))
+        return t
+
+    def stats(self, i: int) -> N.Stats:
+        st = N.Stats()
+        self._check(N.lib.fsr_batch_frame_stats(self._b, i, ctypes.byref(st)))
+        return st
+
+    def mesh(self, i: int) -> Mesh:
+        nv = int(self.stats(i).n_mesh_vertices)
+        pos = np.empty((max(nv, 1), 3), np.float32)
+        nrm = np.empty((max(nv, 1), 3), np.float32)
+        out = ctypes.c_uint64(0)
+        self._check(N.lib.fsr_batch_copy_mesh(self._b, i, pos.ctypes.data, nrm.ctypes.data, nv, ctypes.byref(out)))
+        return Mesh(pos[:nv], nrm[:nv])
+
+
 def read_xyz(path: str):
     """Parses an .xyz file; returns (header, xyz (N,3), density (N,))."""
     hd = N.FrameHeader()

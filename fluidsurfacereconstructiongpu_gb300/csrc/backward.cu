@@ -302,6 +302,37 @@ __global__ void k_field_backward_aniso(BwdArgs a)
     a.gG[3ull * j + 2] = make_float4(gg[6], gg[7], gg[8], 0.f);
 }
 
+// c = sigma det(G) m / rho: adds (sum dL/dphi (1 - q2)^3) dc/dG = that sum
+// times c G^-T (G is symmetric) to dL/dG of each involved particle, after
+// the grouped adjoint has accumulated the sum in gsmooth.w.
+__global__ void k_det_term(BwdArgs a)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n || !a.invol[a.skeys[j]]) return;
+    const float sc = a.gsmooth[j].w;
+    if (sc == 0.f) return;
+    const float4 g0 = a.grec[4ull * j + 1], g1 = a.grec[4ull * j + 2], g2 = a.grec[4ull * j + 3];
+    const float G[9] = {g0.x, g0.y, g0.z, g1.x, g1.y, g1.z, g2.x, g2.y, g2.z};
+    const float det = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
+                      G[2] * (G[3] * G[7] - G[4] * G[6]);
+    if (det == 0.f) return;
+    const float k = sc * g0.w / det;
+    float4* r = a.gG + 3ull * j;
+    float4 r0 = r[0], r1 = r[1], r2 = r[2];
+    r0.x += k * (G[4] * G[8] - G[5] * G[7]);
+    r0.y += k * (G[5] * G[6] - G[3] * G[8]);
+    r0.z += k * (G[3] * G[7] - G[4] * G[6]);
+    r1.x += k * (G[2] * G[7] - G[1] * G[8]);
+    r1.y += k * (G[0] * G[8] - G[2] * G[6]);
+    r1.z += k * (G[1] * G[6] - G[0] * G[7]);
+    r2.x += k * (G[1] * G[5] - G[2] * G[4]);
+    r2.y += k * (G[2] * G[3] - G[0] * G[5]);
+    r2.z += k * (G[0] * G[4] - G[1] * G[3]);
+    r[0] = r0;
+    r[1] = r1;
+    r[2] = r2;
+}
+
 // ---------------------------------------------------------------- covariance / G
 // dL/dC of G = V diag(d) V^T, d_i = cof / s_i, s_i = max(l_i, lmax/4),
 // cof = h_inv cbrt(s_1 s_2 s_3).
@@ -362,10 +393,18 @@ __device__ void g_to_c(const T V[3][3], const T l[3], float h_inv, const float g
                 M[i][k] = gl[i];
                 continue;
             }
-            const T dl = l[i] - l[k];
+            // divided difference (d_i - d_k) / (l_i - l_k) with d = cof / s:
+            // unclamped pairs (s = l > 0) reduce to -cof / (l_i l_k) exactly,
+            // which avoids the cancellation of near-degenerate eigenvalues
             T K;
-            if (fabs(dl) > T(1e-6) * lmax) K = (d[i] - d[k]) / dl;
-            else K = (!clamped[i] && !clamped[k]) ? -cof / (s[i] * s[k]) : T(0);  // limit of a common cof/s
+            if (!clamped[i] && !clamped[k]) {
+                K = -cof / (s[i] * s[k]);
+            } else if (clamped[i] && clamped[k]) {
+                K = T(0);
+            } else {
+                const T dl = l[i] - l[k];
+                K = dl != T(0) ? cof * (s[k] - s[i]) / (s[i] * s[k] * dl) : T(0);
+            }
             M[i][k] = K * P[i][k];
         }
     for (int i = 0; i < 3; ++i)
@@ -563,7 +602,26 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
     k_mark_keys<<<bb, kT, 0, c.stream>>>(a, ctr);
     g_launches += 2;
     if (method == FSR_METHOD_YU13) {
-        k_field_backward_aniso<<<nblk(a.n), kT, 0, c.stream>>>(a);
+        AnisoBwdArgs fb{};
+        fb.sp = a.sp;
+        fb.sc = a.sc;
+        fb.band = a.band;
+        fb.smoothed = a.smoothed;
+        fb.grec = a.grec;
+        fb.ranges = a.ranges;
+        fb.invol = a.invol;
+        fb.cell_rmax = a.cell_rmax;
+        fb.gphi = a.gphi;
+        fb.gkey = a.gkey;
+        fb.gsmooth = a.gsmooth;
+        fb.gG = a.gG;
+        fb.sigma = a.sigma;
+        fb.cap = a.cap_band;
+        if (launch_field_aniso_backward_grouped(c, fb, a.ratio, ctr)) {
+            k_det_term<<<nblk(a.n), kT, 0, c.stream>>>(a);
+        } else {
+            k_field_backward_aniso<<<nblk(a.n), kT, 0, c.stream>>>(a);
+        }
         k_cov_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, *cov);
         k_smooth_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, cov->sorted, cov->mean, cov->ranges, cov->sp, a.n, R,
                                                            lambda);

@@ -24,9 +24,11 @@ struct BwdArgs {
     const uint8_t* invol;
     const float4* smoothed;
     const float4* grec;
+    const uint2* ranges;
+    const float* cell_rmax;  // Yu13: per cell, largest support reach of its particles
     const float4* mv;        // ZB05: per band vertex (mean - v, weight sum)
-    float4* gsmooth;         // dL/d smoothed position (Yu13)
-    float4* gG;              // dL/dG, 3 float4 rows per particle (Yu13)
+    float4* gsmooth;         // dL/d smoothed position (Yu13; zeroed); w: sum dL/dphi (1 - q2)^3
+    float4* gG;              // dL/dG, 3 float4 rows per particle (Yu13; zeroed)
     float4* gmean;           // dL/d mean from the covariance (Yu13)
     float4* gx;              // dL/dx in sorted order (zeroed)
     float iso, h, sigma;

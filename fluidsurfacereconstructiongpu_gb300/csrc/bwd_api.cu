@@ -78,6 +78,10 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     BCK(cudaMemsetAsync(h->gkey.ptr, 0, keys, st));
     BCK(cudaMemsetAsync(h->gx.ptr, 0, 16ull * nn, st));
     BCK(cudaMemsetAsync(h->gscalar.ptr, 0, 16, st));
+    if (p.method == FSR_METHOD_YU13) {
+        BCK(cudaMemsetAsync(h->gsmooth.ptr, 0, 16ull * nn, st));
+        BCK(cudaMemsetAsync(h->gG.ptr, 0, 48ull * nn, st));
+    }
 
     BwdArgs a{};
     a.sp = sp;
@@ -99,6 +103,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     a.invol = (const uint8_t*)h->invol.ptr;
     a.smoothed = (const float4*)h->smoothed.ptr;
     a.grec = (const float4*)h->grec.ptr;
+    a.ranges = (const uint2*)h->ranges.ptr;
+    a.cell_rmax = (const float*)h->cell_rmax.ptr;
     a.mv = (const float4*)h->mv.ptr;
     a.gsmooth = (float4*)h->gsmooth.ptr;
     a.gG = (float4*)h->gG.ptr;
@@ -131,10 +137,12 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     }
     const KernelCtx kc{st, h->num_sms};
     const bool want_radius = grad_particle_radius && (p.method == FSR_METHOD_ZB05 || p.method == FSR_METHOD_AKINCI12);
+    const uint64_t launches0 = g_launches;
     if (n > 0)
         launch_backward(kc, a, &ca, (const Counters*)h->ctr.ptr, (int)p.method, p.smoothing_lambda, R,
                         want_radius ? (float*)h->gscalar.ptr : nullptr, d_grad_xyz);
     BCK(cudaGetLastError());
+    h->stats.n_backward_launches = (uint32_t)(g_launches - launches0);
     if (grad_particle_radius) {
         float r = 0.f;
         if (want_radius) {

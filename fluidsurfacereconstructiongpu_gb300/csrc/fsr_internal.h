@@ -28,6 +28,28 @@ uint32_t bits_for(uint64_t c);
 fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_xyz, const float* d_den,
                      uint64_t n, cudaStream_t st);
 
+// One frame in four steps, so that a batch can queue (and capture) the device
+// work of many frames before it synchronises:
+//   frame_plan     host checks, grids, first capacities
+//   frame_buffers  grows the pooled buffers to the current capacities
+//   frame_enqueue  queues every kernel of the frame on `st` and, last, the
+//                  copy of the Counters block into pinned host memory; it
+//                  never synchronises and allocates nothing
+//   frame_finish   after the stream has been synchronised: reads the
+//                  counters, sets the stats, or grows the capacities and
+//                  asks for a re-run (*retry)
+struct FramePlan {
+    fsr_frame_header hdr{};
+    Grid sp{}, sc{};
+    uint64_t C = 0, V = 0;
+    uint32_t n = 0, nwords = 0;
+};
+fsr_status frame_plan(fsr_handle* h, const fsr_frame_header& hdr, uint64_t n, FramePlan& fp);
+fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp);
+fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz, const float* d_den,
+                         cudaStream_t st, bool timing);
+fsr_status frame_finish(fsr_handle* h, const FramePlan& fp, bool timing, bool* retry);
+
 }  // namespace fsr
 
 struct fsr_handle {
@@ -57,6 +79,9 @@ struct fsr_handle {
     fsr::DevBuf gphi, gkey, gsmooth, gG, gmean, gx, gscalar, tri;
 
     uint32_t cap_band = 0, cap_valid = 0, cap_mesh = 0;
+    int grid_div = 1;                    // grid-stride kernels use num_sms * per_sm / grid_div blocks
+    uint64_t launches_mark = 0;
+    uint32_t launches_frame = 0;
     fsr::Counters* pinned_ctr = nullptr;
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev[FSR_NUM_STAGES] = {};

@@ -34,7 +34,8 @@ inline unsigned blocks_for(uint64_t n, int threads = kThreads)
 inline unsigned persistent_blocks(const KernelCtx& c, uint64_t cap, int per_sm = 8)
 {
     const uint64_t want = (cap + kThreads - 1) / kThreads;
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c.num_sms * per_sm));
+    const uint64_t most = std::max<uint64_t>(1, (uint64_t)c.num_sms * per_sm / std::max(1, c.grid_div));
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, most));
 }
 
 __device__ __forceinline__ void warp_count(uint32_t* counter, bool pred)

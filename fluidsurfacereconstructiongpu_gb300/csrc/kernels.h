@@ -16,6 +16,7 @@ enum class Field : int { kZB05 = 0, kTC01 = 1, kAniso = 2 };
 struct KernelCtx {
     cudaStream_t stream;
     int num_sms;
+    int grid_div = 1;  // grid-stride kernels launch num_sms * per_sm / grid_div blocks (batches run frames side by side)
 };
 
 // spatial hashing: keys[i] = cell id, vals[i] = i.
@@ -94,6 +95,28 @@ void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* c
 // false (nothing launched) when the grid ratio makes a group too large.
 bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& a, const BandView& band, uint32_t ratio,
                                 Counters* ctr);
+
+// Adjoint of the anisotropic field, grouped like the forward pass: adds
+// (dL/dx~, sum dL/dphi (1 - q2)^3) to gsmooth and dL/dG rows (without the
+// det(G) term) to gG; both must start at zero.  Returns false (nothing
+// launched) when the grid ratio makes a group too large.
+struct AnisoBwdArgs {
+    Grid sp, sc;
+    BandView band;
+    const float4* smoothed;
+    const float4* grec;
+    const uint2* ranges;
+    const uint8_t* invol;
+    const float* cell_rmax;
+    const float* gphi;
+    const uint8_t* gkey;
+    float4* gsmooth;
+    float4* gG;
+    float sigma;
+    uint32_t cap;
+};
+bool launch_field_aniso_backward_grouped(const KernelCtx& c, const AnisoBwdArgs& a, uint32_t ratio,
+                                         const Counters* ctr);
 
 struct McArgs {
     Grid sc;

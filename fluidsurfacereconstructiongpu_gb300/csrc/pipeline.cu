@@ -180,38 +180,46 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 
 namespace fsr {
 
-fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_xyz, const float* d_den,
-                     uint64_t n64, cudaStream_t st)
+fsr_status frame_plan(fsr_handle* h, const fsr_frame_header& hdr, uint64_t n64, FramePlan& fp)
 {
     const fsr_params& p = h->params;
     if (n64 >= 0xFFFFFFFFull) return fail(h, FSR_ERR_TOO_LARGE, "too many particles: %llu", (unsigned long long)n64);
-    const uint32_t n = (uint32_t)n64;
     if (!(hdr.kernel_radius > 0.0f) || !std::isfinite(hdr.kernel_radius))
         return fail(h, FSR_ERR_INVALID_ARGUMENT, "kernel radius must be positive");
-    Grid sp{}, sc{};
-    uint64_t C = 0, V = 0;
-    if (!derive_grids(hdr, p, sp, sc, nullptr, C, V))
+    fp = FramePlan{};
+    fp.hdr = hdr;
+    fp.n = (uint32_t)n64;
+    if (!derive_grids(hdr, p, fp.sp, fp.sc, nullptr, fp.C, fp.V))
         return fail(h, FSR_ERR_INVALID_ARGUMENT, "invalid grid (bounding box, kernel radius or ratio)");
-    if (C >= 0xFFFFFFFFull || V >= 0xFFFFFFFFull)
-        return fail(h, FSR_ERR_TOO_LARGE, "grid too large: %llu cells, %llu vertices", (unsigned long long)C,
-                    (unsigned long long)V);
-    const uint32_t nwords = (uint32_t)((V + 31) / 32);
-    const bool yu13 = p.method == FSR_METHOD_YU13;
-    const bool akinci = p.method == FSR_METHOD_AKINCI12;
-    const bool keep = (p.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
-    const bool timing = (p.flags & FSR_FLAG_STAGE_TIMING) != 0;
-    const uint32_t nn = std::max<uint32_t>(n, 1);
-
+    if (fp.C >= 0xFFFFFFFFull || fp.V >= 0xFFFFFFFFull)
+        return fail(h, FSR_ERR_TOO_LARGE, "grid too large: %llu cells, %llu vertices", (unsigned long long)fp.C,
+                    (unsigned long long)fp.V);
+    fp.nwords = (uint32_t)((fp.V + 31) / 32);
     // capacities of the device-sized arrays
-    if (h->cap_band == 0) h->cap_band = (uint32_t)std::min<uint64_t>(V, std::max<uint64_t>(1u << 20, 24ull * n));
+    if (p.flags & FSR_FLAG_SMALL_POOLS) {
+        if (h->cap_band == 0) h->cap_band = (uint32_t)std::min<uint64_t>(fp.V, 4096);
+        if (h->cap_valid == 0) h->cap_valid = 1024;
+        if (h->cap_mesh == 0) h->cap_mesh = 4096;
+    }
+    if (h->cap_band == 0) h->cap_band = (uint32_t)std::min<uint64_t>(fp.V, std::max<uint64_t>(1u << 20, 24ull * fp.n));
     if (h->cap_valid == 0) h->cap_valid = std::max<uint32_t>(1u << 18, h->cap_band / 4);
     if (h->cap_mesh == 0) h->cap_mesh = std::max<uint32_t>(1u << 20, 4u * h->cap_valid);
+    return FSR_OK;
+}
 
+fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
+{
+    const fsr_params& p = h->params;
+    const bool yu13 = p.method == FSR_METHOD_YU13;
+    const bool keep = (p.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
+    const bool timing = (p.flags & FSR_FLAG_STAGE_TIMING) != 0;
+    const uint64_t nn = std::max<uint32_t>(fp.n, 1);
+    const uint64_t C = fp.C, nwords = fp.nwords;
     CK(h->keys0.ensure(4ull * nn));
     CK(h->vals0.ensure(4ull * nn));
     CK(h->keys1.ensure(4ull * nn));
     CK(h->vals1.ensure(4ull * nn));
-    CK(h->radix_tmp.ensure(4ull * radix_scratch_words(nn)));
+    CK(h->radix_tmp.ensure(4ull * radix_scratch_words((uint32_t)nn)));
     CK(h->sorted.ensure(16ull * nn));
     CK(h->ranges.ensure(8ull * C));
     CK(h->occ.ensure(C));
@@ -226,231 +234,263 @@ fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_
         CK(h->smoothed.ensure(16ull * nn));
         CK(h->grec.ensure(64ull * nn));
     }
-    if (akinci) CK(h->psurf.ensure(nn));
+    if (p.method == FSR_METHOD_AKINCI12) CK(h->psurf.ensure(nn));
     if (keep) CK(h->pflags.ensure(4ull * nn));
     if (!h->pinned_ctr) CK(cudaMallocHost(&h->pinned_ctr, sizeof(Counters)));
     if (timing && !h->ev_start) {
         CK(cudaEventCreate(&h->ev_start));
         for (auto& e : h->ev) CK(cudaEventCreate(&e));
     }
+    const uint64_t scan_words = std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
+    CK(h->scan_tmp.ensure(4ull * scan_words));
+    CK(h->sv.ensure(4ull * h->cap_band));
+    CK(h->phi.ensure(4ull * h->cap_band));
+    CK(h->mc.ensure(4ull * h->cap_band));
+    CK(h->vofs.ensure(4ull * h->cap_band));
+    CK(h->qpos.ensure(4ull * h->cap_band));
+    CK(h->valid.ensure(4ull * h->cap_valid));
+    CK(h->mesh_pos.ensure(12ull * h->cap_mesh));
+    CK(h->mesh_nrm.ensure(12ull * h->cap_mesh));
+    if (!yu13 && p.method != FSR_METHOD_TC01) CK(h->mv.ensure(16ull * h->cap_band));
+    return FSR_OK;
+}
 
-    const KernelCtx kc{st, h->num_sms};
+fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz, const float* d_den,
+                         cudaStream_t st, bool timing)
+{
+    const fsr_params& p = h->params;
+    const fsr_frame_header& hdr = fp.hdr;
+    const Grid sp = fp.sp, sc = fp.sc;
+    const uint64_t C = fp.C;
+    const uint32_t n = fp.n, nwords = fp.nwords;
+    const bool yu13 = p.method == FSR_METHOD_YU13;
+    const bool akinci = p.method == FSR_METHOD_AKINCI12;
+    const bool keep = (p.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
+    const KernelCtx kc{st, h->num_sms, h->grid_div};
     Counters* ctr = (Counters*)h->ctr.ptr;
     const float h_r = hdr.kernel_radius;
     const float h2 = h_r * h_r;
 
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        const uint64_t scan_words =
-            std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
-        CK(h->scan_tmp.ensure(4ull * scan_words));
-        CK(h->sv.ensure(4ull * h->cap_band));
-        CK(h->phi.ensure(4ull * h->cap_band));
-        CK(h->mc.ensure(4ull * h->cap_band));
-        CK(h->vofs.ensure(4ull * h->cap_band));
-        CK(h->qpos.ensure(4ull * h->cap_band));
-        CK(h->valid.ensure(4ull * h->cap_valid));
-        CK(h->mesh_pos.ensure(12ull * h->cap_mesh));
-        CK(h->mesh_nrm.ensure(12ull * h->cap_mesh));
-        if (!yu13 && p.method != FSR_METHOD_TC01) CK(h->mv.ensure(16ull * h->cap_band));
+    auto mark = [&](int stage) {
+        if (timing) cudaEventRecord(h->ev[stage], st);
+    };
+    if (timing) cudaEventRecord(h->ev_start, st);
 
-        auto mark = [&](int stage) {
-            if (timing) cudaEventRecord(h->ev[stage], st);
-        };
-        if (timing) cudaEventRecord(h->ev_start, st);
+    h->launches_mark = g_launches;
+    CK(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
+    CK(cudaMemsetAsync(h->ranges.ptr, 0xFF, 8ull * C, st));
+    CK(cudaMemsetAsync(h->occ.ptr, 0, C, st));
+    CK(cudaMemsetAsync(h->bits.ptr, 0, 4ull * nwords + 4, st));
+    if (yu13) CK(cudaMemsetAsync(h->cell_rmax.ptr, 0, 4ull * C, st));
 
-        const uint64_t launches0 = g_launches;
-        CK(cudaMemsetAsync(ctr, 0, sizeof(Counters), st));
-        CK(cudaMemsetAsync(h->ranges.ptr, 0xFF, 8ull * C, st));
-        CK(cudaMemsetAsync(h->occ.ptr, 0, C, st));
-        CK(cudaMemsetAsync(h->bits.ptr, 0, 4ull * nwords + 4, st));
-        if (yu13) CK(cudaMemsetAsync(h->cell_rmax.ptr, 0, 4ull * C, st));
+    // ---- spatial hashing (ReconstructorGPU.cpp:292-313)
+    uint32_t* k0 = (uint32_t*)h->keys0.ptr;
+    uint32_t* v0 = (uint32_t*)h->vals0.ptr;
+    uint32_t* k1 = (uint32_t*)h->keys1.ptr;
+    uint32_t* v1 = (uint32_t*)h->vals1.ptr;
+    launch_hash(kc, d_xyz, n, sp, k0, v0, ctr);
+    cudaError_t se = cudaSuccess;
+    const int which = radix_sort_pairs(k0, v0, k1, v1, n, bits_for(C), (uint32_t*)h->radix_tmp.ptr, st, &se);
+    if (se != cudaSuccess) return cuda_fail(h, se, "radix sort");
+    const uint32_t* skeys = which ? k1 : k0;
+    const uint32_t* perm = which ? v1 : v0;
+    h->perm_ptr = perm;
+    h->skeys_ptr = skeys;
+    mark(0);
+    float4* sorted = (float4*)h->sorted.ptr;
+    uint2* ranges = (uint2*)h->ranges.ptr;
+    uint8_t* occ = (uint8_t*)h->occ.ptr;
+    launch_ranges_gather(kc, skeys, perm, n, d_xyz, d_den, sorted, ranges, occ);
+    mark(1);
 
-        // ---- spatial hashing (ReconstructorGPU.cpp:292-313)
-        uint32_t* k0 = (uint32_t*)h->keys0.ptr;
-        uint32_t* v0 = (uint32_t*)h->vals0.ptr;
-        uint32_t* k1 = (uint32_t*)h->keys1.ptr;
-        uint32_t* v1 = (uint32_t*)h->vals1.ptr;
-        launch_hash(kc, d_xyz, n, sp, k0, v0, ctr);
-        cudaError_t se = cudaSuccess;
-        const int which = radix_sort_pairs(k0, v0, k1, v1, n, bits_for(C), (uint32_t*)h->radix_tmp.ptr, st, &se);
-        if (se != cudaSuccess) return cuda_fail(h, se, "radix sort");
-        const uint32_t* skeys = which ? k1 : k0;
-        const uint32_t* perm = which ? v1 : v0;
-        h->perm_ptr = perm;
-        h->skeys_ptr = skeys;
-        mark(0);
-        float4* sorted = (float4*)h->sorted.ptr;
-        uint2* ranges = (uint2*)h->ranges.ptr;
-        uint8_t* occ = (uint8_t*)h->occ.ptr;
-        launch_ranges_gather(kc, skeys, perm, n, d_xyz, d_den, sorted, ranges, occ);
-        mark(1);
+    // ---- surface cells / particles
+    uint8_t* surf = (uint8_t*)h->surf.ptr;
+    uint8_t* psurf = akinci ? (uint8_t*)h->psurf.ptr : nullptr;
+    if (akinci) {
+        launch_colorfield(kc, sorted, n, ranges, sp, h_r, h2, hdr.particle_mass, psurf);
+    } else {
+        launch_surface_cells(kc, sp, occ, surf);
+        if (yu13) launch_involved_cells(kc, sp, occ, surf, (uint8_t*)h->invol.ptr);
+    }
+    if (keep) launch_particle_flags(kc, skeys, surf, psurf, n, (uint32_t*)h->pflags.ptr);
+    mark(2);
 
-        // ---- surface cells / particles
-        uint8_t* surf = (uint8_t*)h->surf.ptr;
-        uint8_t* psurf = akinci ? (uint8_t*)h->psurf.ptr : nullptr;
-        if (akinci) {
-            launch_colorfield(kc, sorted, n, ranges, sp, h_r, h2, hdr.particle_mass, psurf);
-        } else {
-            launch_surface_cells(kc, sp, occ, surf);
-            if (yu13) launch_involved_cells(kc, sp, occ, surf, (uint8_t*)h->invol.ptr);
+    // ---- narrow band
+    uint32_t* bits = (uint32_t*)h->bits.ptr;
+    uint32_t* prefix = (uint32_t*)h->prefix.ptr;
+    launch_band_stamp(kc, sorted, skeys, surf, psurf, n, sc, band_threshold(h_r), bits, ctr);
+    mark(3);
+    CK(scan_u32(bits, prefix, nwords, nullptr, nwords, &ctr->n_band, ScanInput::kPopcount,
+                (uint32_t*)h->scan_tmp.ptr, st));
+    uint32_t* sv = (uint32_t*)h->sv.ptr;
+    launch_band_list(kc, bits, prefix, nwords, sv, h->cap_band, ctr);
+    mark(4);
+
+    // ---- field
+    float* phi = (float*)h->phi.ptr;
+    if (yu13) {
+        const float R = h_r * p.aniso_radius_over_h;
+        launch_smooth(kc, sorted, n, ranges, sp, R, p.smoothing_lambda, hdr.particle_mass, (float4*)h->mean.ptr,
+                      (float4*)h->smoothed.ptr);
+        mark(5);
+        CovArgs ca{};
+        ca.sp = sp;
+        ca.sorted = sorted;
+        ca.mean = (const float4*)h->mean.ptr;
+        ca.smoothed = (const float4*)h->smoothed.ptr;
+        ca.ranges = ranges;
+        ca.skeys = skeys;
+        ca.invol = (const uint8_t*)h->invol.ptr;
+        ca.grec = (float4*)h->grec.ptr;
+        ca.cell_rmax = (float*)h->cell_rmax.ptr;
+        ca.n = n;
+        ca.R = R;
+        ca.h = h_r;
+        ca.h2 = h2;
+        ca.h_inv = (float)(1.0 / (double)h_r);
+        ca.mass = hdr.particle_mass;
+        ca.sigma = 315.0f / (64.0f * 3.1415926535898f);
+        ca.min_neighbors = p.min_neighbors;
+        launch_cov(kc, ca, ctr);
+        mark(6);
+        AnisoFieldArgs fa{};
+        fa.sp = sp;
+        fa.sc = sc;
+        fa.smoothed = (const float4*)h->smoothed.ptr;
+        fa.grec = (const float4*)h->grec.ptr;
+        fa.ranges = ranges;
+        fa.invol = (const uint8_t*)h->invol.ptr;
+        fa.occ = occ;
+        fa.cell_rmax = (const float*)h->cell_rmax.ptr;
+        fa.sv = sv;
+        fa.phi = phi;
+        fa.sigma = ca.sigma;
+        fa.cap = h->cap_band;
+        if (!launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr))
+            launch_field_aniso(kc, fa, ctr);
+    } else {
+        mark(5);
+        mark(6);
+        IsoFieldArgs fa{};
+        fa.sp = sp;
+        fa.sc = sc;
+        fa.sorted = sorted;
+        fa.ranges = ranges;
+        fa.sv = sv;
+        fa.phi = phi;
+        fa.h = h_r;
+        fa.h2 = h2;
+        fa.inv_h2 = 1.0f / h2;
+        fa.rp = hdr.particle_radius;
+        fa.mv = p.method == FSR_METHOD_TC01 ? nullptr : (float4*)h->mv.ptr;
+        fa.cap = h->cap_band;
+        launch_field_iso(kc, p.method == FSR_METHOD_TC01 ? Field::kTC01 : Field::kZB05, fa, ctr);
+    }
+    mark(7);
+
+    // ---- marching cubes
+    McArgs ma{};
+    ma.sc = sc;
+    ma.band = BandView{bits, prefix, phi};
+    ma.sv = sv;
+    ma.mc = (uint32_t*)h->mc.ptr;
+    ma.vofs = (const uint32_t*)h->vofs.ptr;
+    ma.qpos = (const uint32_t*)h->qpos.ptr;
+    ma.valid = (uint32_t*)h->valid.ptr;
+    ma.out_pos = (float*)h->mesh_pos.ptr;
+    ma.out_nrm = (float*)h->mesh_nrm.ptr;
+    ma.iso = p.iso_value;
+    ma.fill = yu13 ? __builtin_bit_cast(float, 0x64646464u) : 0.0f;  // memset values (Yu13.cpp:264, ZB05.cpp:324)
+    ma.host_mc = akinci ? 1 : 0;
+    ma.cap_band = h->cap_band;
+    ma.cap_valid = h->cap_valid;
+    ma.cap_mesh = h->cap_mesh;
+    launch_mc_classify(kc, ma, ctr);
+    mark(8);
+    CK(scan_u32(ma.mc, (uint32_t*)h->vofs.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_mesh_verts,
+                ScanInput::kLowByte, (uint32_t*)h->scan_tmp.ptr, st));
+    CK(scan_u32(ma.mc, (uint32_t*)h->qpos.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_valid,
+                ScanInput::kLowByteNonzero, (uint32_t*)h->scan_tmp.ptr, st));
+    launch_valid_list(kc, ma, ctr);
+    mark(9);
+    launch_mc_generate(kc, ma, ctr);
+    mark(10);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->pinned_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    mark(11);
+    h->launches_frame = (uint32_t)(g_launches - h->launches_mark);
+    return FSR_OK;
+}
+
+fsr_status frame_finish(fsr_handle* h, const FramePlan& fp, bool timing, bool* retry)
+{
+    *retry = false;
+    const Counters& hc = *h->pinned_ctr;
+    if (hc.out_of_grid)
+        return fail(h, FSR_ERR_OUT_OF_GRID, "%u particle(s) outside the expanded bounding box", hc.out_of_grid);
+    if (hc.overflow) {
+        if (hc.overflow & 1u)
+            h->cap_band = (uint32_t)std::min<uint64_t>(fp.V, (uint64_t)hc.need_band * 5 / 4 + 1024);
+        if (hc.overflow & 2u) h->cap_valid = std::min<uint32_t>(h->cap_band, hc.need_valid + hc.need_valid / 4 + 1024);
+        if (hc.overflow & 4u)
+            h->cap_mesh = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)hc.need_mesh * 5 / 4 + 4096);
+        if (hc.overflow & 1u) {
+            // a band overflow also invalidated the later stages' sizes
+            h->cap_valid = std::max<uint32_t>(h->cap_valid, std::min<uint32_t>(h->cap_band, h->cap_band / 4));
         }
-        if (keep) launch_particle_flags(kc, skeys, surf, psurf, n, (uint32_t*)h->pflags.ptr);
-        mark(2);
-
-        // ---- narrow band
-        uint32_t* bits = (uint32_t*)h->bits.ptr;
-        uint32_t* prefix = (uint32_t*)h->prefix.ptr;
-        launch_band_stamp(kc, sorted, skeys, surf, psurf, n, sc, band_threshold(h_r), bits, ctr);
-        mark(3);
-        CK(scan_u32(bits, prefix, nwords, nullptr, nwords, &ctr->n_band, ScanInput::kPopcount,
-                    (uint32_t*)h->scan_tmp.ptr, st));
-        uint32_t* sv = (uint32_t*)h->sv.ptr;
-        launch_band_list(kc, bits, prefix, nwords, sv, h->cap_band, ctr);
-        mark(4);
-
-        // ---- field
-        float* phi = (float*)h->phi.ptr;
-        if (yu13) {
-            const float R = h_r * p.aniso_radius_over_h;
-            launch_smooth(kc, sorted, n, ranges, sp, R, p.smoothing_lambda, hdr.particle_mass, (float4*)h->mean.ptr,
-                          (float4*)h->smoothed.ptr);
-            mark(5);
-            CovArgs ca{};
-            ca.sp = sp;
-            ca.sorted = sorted;
-            ca.mean = (const float4*)h->mean.ptr;
-            ca.smoothed = (const float4*)h->smoothed.ptr;
-            ca.ranges = ranges;
-            ca.skeys = skeys;
-            ca.invol = (const uint8_t*)h->invol.ptr;
-            ca.grec = (float4*)h->grec.ptr;
-            ca.cell_rmax = (float*)h->cell_rmax.ptr;
-            ca.n = n;
-            ca.R = R;
-            ca.h = h_r;
-            ca.h2 = h2;
-            ca.h_inv = (float)(1.0 / (double)h_r);
-            ca.mass = hdr.particle_mass;
-            ca.sigma = 315.0f / (64.0f * 3.1415926535898f);
-            ca.min_neighbors = p.min_neighbors;
-            launch_cov(kc, ca, ctr);
-            mark(6);
-            AnisoFieldArgs fa{};
-            fa.sp = sp;
-            fa.sc = sc;
-            fa.smoothed = (const float4*)h->smoothed.ptr;
-            fa.grec = (const float4*)h->grec.ptr;
-            fa.ranges = ranges;
-            fa.invol = (const uint8_t*)h->invol.ptr;
-            fa.occ = occ;
-            fa.cell_rmax = (const float*)h->cell_rmax.ptr;
-            fa.sv = sv;
-            fa.phi = phi;
-            fa.sigma = ca.sigma;
-            fa.cap = h->cap_band;
-            if (!launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr))
-                launch_field_aniso(kc, fa, ctr);
-        } else {
-            mark(5);
-            mark(6);
-            IsoFieldArgs fa{};
-            fa.sp = sp;
-            fa.sc = sc;
-            fa.sorted = sorted;
-            fa.ranges = ranges;
-            fa.sv = sv;
-            fa.phi = phi;
-            fa.h = h_r;
-            fa.h2 = h2;
-            fa.inv_h2 = 1.0f / h2;
-            fa.rp = hdr.particle_radius;
-            fa.mv = p.method == FSR_METHOD_TC01 ? nullptr : (float4*)h->mv.ptr;
-            fa.cap = h->cap_band;
-            launch_field_iso(kc, p.method == FSR_METHOD_TC01 ? Field::kTC01 : Field::kZB05, fa, ctr);
-        }
-        mark(7);
-
-        // ---- marching cubes
-        McArgs ma{};
-        ma.sc = sc;
-        ma.band = BandView{bits, prefix, phi};
-        ma.sv = sv;
-        ma.mc = (uint32_t*)h->mc.ptr;
-        ma.vofs = (const uint32_t*)h->vofs.ptr;
-        ma.qpos = (const uint32_t*)h->qpos.ptr;
-        ma.valid = (uint32_t*)h->valid.ptr;
-        ma.out_pos = (float*)h->mesh_pos.ptr;
-        ma.out_nrm = (float*)h->mesh_nrm.ptr;
-        ma.iso = p.iso_value;
-        ma.fill = yu13 ? __builtin_bit_cast(float, 0x64646464u) : 0.0f;  // memset values (Yu13.cpp:264, ZB05.cpp:324)
-        ma.host_mc = akinci ? 1 : 0;
-        ma.cap_band = h->cap_band;
-        ma.cap_valid = h->cap_valid;
-        ma.cap_mesh = h->cap_mesh;
-        launch_mc_classify(kc, ma, ctr);
-        mark(8);
-        CK(scan_u32(ma.mc, (uint32_t*)h->vofs.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_mesh_verts,
-                    ScanInput::kLowByte, (uint32_t*)h->scan_tmp.ptr, st));
-        CK(scan_u32(ma.mc, (uint32_t*)h->qpos.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_valid,
-                    ScanInput::kLowByteNonzero, (uint32_t*)h->scan_tmp.ptr, st));
-        launch_valid_list(kc, ma, ctr);
-        mark(9);
-        launch_mc_generate(kc, ma, ctr);
-        mark(10);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(h->pinned_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-        mark(11);
-        CK(cudaStreamSynchronize(st));
-
-        const Counters& hc = *h->pinned_ctr;
-        if (hc.out_of_grid)
-            return fail(h, FSR_ERR_OUT_OF_GRID, "%u particle(s) outside the expanded bounding box", hc.out_of_grid);
-        if (hc.overflow) {
-            if (hc.overflow & 1u) h->cap_band = (uint32_t)std::min<uint64_t>(V, (uint64_t)hc.need_band * 5 / 4 + 1024);
-            if (hc.overflow & 2u) h->cap_valid = std::min<uint32_t>(h->cap_band, hc.need_valid + hc.need_valid / 4 + 1024);
-            if (hc.overflow & 4u)
-                h->cap_mesh = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)hc.need_mesh * 5 / 4 + 4096);
-            if (hc.overflow & 1u) {
-                // a band overflow also invalidated the later stages' sizes
-                h->cap_valid = std::max<uint32_t>(h->cap_valid, std::min<uint32_t>(h->cap_band, h->cap_band / 4));
-            }
-            h->stats.n_retries++;
-            continue;
-        }
-        // stats
-        fsr_stats& s = h->stats;
-        s.n_particles = n;
-        s.n_cells = C;
-        s.n_grid_vertices = V;
-        s.n_surface_particles = hc.n_surface;
-        s.n_involved_particles = hc.n_involved;
-        s.n_band_vertices = hc.n_band;
-        s.n_valid_cubes = hc.n_valid;
-        s.n_mesh_vertices = hc.n_mesh_verts;
-        s.n_fp64_fallbacks = hc.n_fp64;
-        s.n_kernel_launches = (uint32_t)(g_launches - launches0);
-        for (int a = 0; a < 3; ++a) {
-            s.spatial_res[a] = sp.res[a];
-            s.scalar_res[a] = sc.res[a];
-        }
-        if (timing) {
-            float prev = 0.f;
-            for (int i = 0; i < FSR_NUM_STAGES; ++i) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, h->ev_start, h->ev[i]);
-                s.stage_ms[i] = ms - prev;
-                prev = ms;
-            }
-            s.total_ms = prev;
-        }
-        h->frame_ready = true;
-        h->grid_sp = sp;
-        h->grid_sc = sc;
-        h->n_last = n;
-        h->C_last = C;
-        h->V_last = V;
-        h->hdr_last = hdr;
+        h->stats.n_retries++;
+        *retry = true;
         return FSR_OK;
+    }
+    fsr_stats& s = h->stats;
+    s.n_particles = fp.n;
+    s.n_cells = fp.C;
+    s.n_grid_vertices = fp.V;
+    s.n_surface_particles = hc.n_surface;
+    s.n_involved_particles = hc.n_involved;
+    s.n_band_vertices = hc.n_band;
+    s.n_valid_cubes = hc.n_valid;
+    s.n_mesh_vertices = hc.n_mesh_verts;
+    s.n_fp64_fallbacks = hc.n_fp64;
+    s.n_kernel_launches = h->launches_frame;
+    s.n_backward_launches = 0;
+    for (int a = 0; a < 3; ++a) {
+        s.spatial_res[a] = fp.sp.res[a];
+        s.scalar_res[a] = fp.sc.res[a];
+    }
+    if (timing) {
+        float prev = 0.f;
+        for (int i = 0; i < FSR_NUM_STAGES; ++i) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, h->ev_start, h->ev[i]);
+            s.stage_ms[i] = ms - prev;
+            prev = ms;
+        }
+        s.total_ms = prev;
+    }
+    h->frame_ready = true;
+    h->grid_sp = fp.sp;
+    h->grid_sc = fp.sc;
+    h->n_last = fp.n;
+    h->C_last = fp.C;
+    h->V_last = fp.V;
+    h->hdr_last = fp.hdr;
+    return FSR_OK;
+}
+
+fsr_status run_frame(fsr_handle* h, const fsr_frame_header& hdr, const float* d_xyz, const float* d_den,
+                     uint64_t n64, cudaStream_t st)
+{
+    FramePlan fp;
+    fsr_status s = frame_plan(h, hdr, n64, fp);
+    if (s != FSR_OK) return s;
+    const bool timing = (h->params.flags & FSR_FLAG_STAGE_TIMING) != 0;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        if ((s = frame_buffers(h, fp)) != FSR_OK) return s;
+        if ((s = frame_enqueue(h, fp, d_xyz, d_den, st, timing)) != FSR_OK) return s;
+        CK(cudaStreamSynchronize(st));
+        bool retry = false;
+        if ((s = frame_finish(h, fp, timing, &retry)) != FSR_OK || !retry) return s;
     }
     return fail(h, FSR_ERR_OUT_OF_MEMORY, "capacity growth did not converge");
 }

@@ -67,6 +67,10 @@ typedef struct fsr_params {
 #define FSR_FLAG_KEEP_INTERMEDIATES 0x1u
 /* Record per-stage CUDA event times (fsr_stats.stage_ms). */
 #define FSR_FLAG_STAGE_TIMING 0x2u
+/* Start the band, valid-cube and mesh pools at a few thousand entries
+ * instead of 2^20 (they grow on demand, re-running the frame once): for
+ * memory-tight callers and batches of many small frames. */
+#define FSR_FLAG_SMALL_POOLS 0x4u
 
 /* The .xyz header (data_format.txt:1-15; ReconstructorGPU.cpp:215-251). */
 typedef struct fsr_frame_header {
@@ -93,6 +97,7 @@ typedef struct fsr_stats {
     uint32_t n_fp64_fallbacks;     /* Yu13: eigen-solves redone in FP64 */
     uint32_t n_retries;            /* frame re-runs after a capacity grow */
     uint32_t n_kernel_launches;    /* kernels launched by the last frame (its final attempt) */
+    uint32_t n_backward_launches;  /* kernels launched by the last fsr_backward call */
     float stage_ms[FSR_NUM_STAGES];/* with FSR_FLAG_STAGE_TIMING */
     float total_ms;
 } fsr_stats;
@@ -212,6 +217,76 @@ fsr_status fsr_spatial_hash_noalloc(const fsr_frame_header* hdr, float cell_size
                                     float* d_sorted_xyz, float* d_sorted_density,
                                     uint32_t* d_cell_ranges, uint64_t cell_capacity, uint32_t* d_perm,
                                     uint32_t* d_out_of_grid, uint64_t* n_cells, void* stream);
+
+/* ---- batches of frames ---------------------------------------------- */
+
+/* Many independent frames (uneven particle counts, mixed methods) in one
+ * CUDA graph launch.  The reference reconstructs one frame per call
+ * (ReconstructorGPU.cpp:25-79: beginFrame / frameMove / endFrame, each
+ * stage followed by a device synchronisation); a batch queues every frame's
+ * kernels without host round trips, spreads the frames over `lanes`
+ * concurrent streams inside the graph (size-balanced: longest frame first
+ * onto the least loaded lane) and synchronises once for the whole batch.
+ * Every frame gives exactly the results of fsr_reconstruct on the same
+ * particles with the same parameters: batching changes no arithmetic.
+ *
+ * The first call with a new frame set (count, particle counts, methods,
+ * headers) plans the batch: each frame runs once on its own to size its
+ * buffers, then the autotuner times candidate lane counts and grid sizes
+ * (grid-stride kernels launch num_sms * k / grid_div blocks) on the real
+ * frames and keeps the fastest graph.  Later calls with the same shape copy
+ * the new particles into the batch's buffers and replay that graph.  The
+ * spatial cell size and the band width are parameters of the reconstruction
+ * (they change the mesh), so the autotuner leaves them alone. */
+typedef struct fsr_batch fsr_batch;
+
+typedef struct fsr_batch_frame {
+    fsr_frame_header header;
+    uint32_t method;          /* fsr_method; the batch's parameters for it */
+    uint32_t reserved;        /* 0 */
+    uint64_t n_particles;
+    const float* xyz;         /* n x 3, device or host (unified addressing) */
+    const float* density;     /* n */
+} fsr_batch_frame;
+
+typedef struct fsr_batch_tuning {
+    uint32_t lanes;               /* concurrent streams inside the graph */
+    uint32_t grid_div;            /* grid-stride kernels: num_sms * k / grid_div blocks */
+    uint32_t n_candidates;        /* configurations the autotuner timed */
+    uint32_t kernels_per_launch;  /* kernel nodes in one graph launch */
+    float graph_ms;               /* one graph launch (the autotuner's best) */
+    float frames_ms;              /* the same frames one after another, one
+                                     synchronised fsr_reconstruct-style run each */
+} fsr_batch_tuning;
+
+/* params: four fsr_params indexed by fsr_method (NULL: fsr_default_params
+ * for each); of their flags only FSR_FLAG_SMALL_POOLS is kept (no stage
+ * timing or intermediates inside graphs). */
+fsr_status fsr_batch_create(const fsr_params* params, int device, fsr_batch** out);
+void fsr_batch_destroy(fsr_batch* b);
+const char* fsr_batch_last_error(const fsr_batch* b);
+
+#define FSR_BATCH_RETUNE 0x1u      /* plan and autotune again even if the shape is unchanged */
+#define FSR_BATCH_NO_AUTOTUNE 0x2u /* plan with lanes = min(count, 8), grid_div = 1 */
+
+/* Reconstructs frames[0 .. count).  The particles are copied (one
+ * cudaMemcpyAsync per array, on `stream`) into buffers the batch owns, the
+ * graph is launched on `stream`, and the call returns after that stream has
+ * been synchronised once.  A frame whose band or mesh outgrew its planned
+ * capacity is re-sized and the batch re-run (counted in each frame's
+ * fsr_stats.n_retries).  The first failing frame's status is returned;
+ * fsr_batch_last_error names it. */
+fsr_status fsr_reconstruct_batch(fsr_batch* b, const fsr_batch_frame* frames, uint32_t count, uint32_t flags,
+                                 void* stream);
+fsr_status fsr_batch_get_tuning(const fsr_batch* b, fsr_batch_tuning* out);
+fsr_status fsr_batch_frame_stats(const fsr_batch* b, uint32_t frame, fsr_stats* out);
+/* Device pointers to frame `frame`'s triangle soup; valid until the next
+ * fsr_reconstruct_batch or fsr_batch_destroy. */
+fsr_status fsr_batch_mesh_device(const fsr_batch* b, uint32_t frame, const float** d_pos, const float** d_nrm,
+                                 uint64_t* n_vertices);
+/* Copies frame `frame`'s mesh to host or device memory (synchronous). */
+fsr_status fsr_batch_copy_mesh(const fsr_batch* b, uint32_t frame, float* pos, float* nrm, uint64_t capacity,
+                               uint64_t* n_vertices);
 
 /* ---- file formats -------------------------------------------------- */
 
