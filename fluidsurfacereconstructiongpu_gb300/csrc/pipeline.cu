@@ -653,6 +653,14 @@ fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out)
     return FSR_OK;
 }
 
+fsr_status fsr_get_frame_header(const fsr_handle* h, fsr_frame_header* out)
+{
+    if (!h || !out) return FSR_ERR_INVALID_ARGUMENT;
+    if (!h->frame_ready) return FSR_ERR_NOT_READY;
+    *out = h->hdr_last;
+    return FSR_OK;
+}
+
 fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes, uint64_t* bytes_needed)
 {
     if (!h) return FSR_ERR_INVALID_ARGUMENT;

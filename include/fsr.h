@@ -160,6 +160,9 @@ fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, float* d_gr
                         float* grad_particle_radius, void* stream);
 
 fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out);
+/* The last reconstructed frame's header (as read from its .xyz file on the
+ * file-driven path). */
+fsr_status fsr_get_frame_header(const fsr_handle* h, fsr_frame_header* out);
 
 /* Intermediates of the last frame (requires FSR_FLAG_KEEP_INTERMEDIATES for
  * the arrays marked *).  With dst == NULL only *bytes_needed is set. */
