@@ -28,7 +28,11 @@ namespace {
 
 constexpr int kBT = 256;            // threads per block
 constexpr int kWarps = kBT / 32;
-constexpr int kChunk = 256;         // candidate records per shared-memory chunk
+#ifndef FSR_FIELD_CHUNK
+#define FSR_FIELD_CHUNK 128
+#endif
+constexpr int kChunk = FSR_FIELD_CHUNK;  // candidate records per shared-memory chunk (a multiple of 32)
+static_assert(kChunk % 32 == 0 && kChunk <= 65536, "chunk indices are 16-bit, warp lists step by 32");
 constexpr int kMaxCells = 125;      // 5 x 5 x 5 window
 
 struct GroupArgs {
@@ -170,13 +174,16 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ grec, con
 __global__ void k_field_aniso_grouped(GroupArgs a, uint32_t ratio, const Counters* ctr)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t ntile_cap = (a.vlist_cap + 31) / 32;
     float4* rec = reinterpret_cast<float4*>(smem);                         // kChunk * 4 float4
-    uint16_t* wlist = reinterpret_cast<uint16_t*>(rec + 4 * kChunk);       // kWarps * kChunk
+    float4* tbox = rec + 4 * kChunk;                                       // per 32-vertex tile: lo, hi
+    uint32_t* vid = reinterpret_cast<uint32_t*>(tbox + 2 * ntile_cap);     // vertex list: grid vertex id
+    uint32_t* vrank = vid + a.vlist_cap;                                   // vertex list: band rank
+    float* vsum = reinterpret_cast<float*>(vrank + a.vlist_cap);           // per vertex partial sum
+    uint16_t* wlist = reinterpret_cast<uint16_t*>(vsum + a.vlist_cap);     // kWarps * kChunk
     uint32_t* cstart = reinterpret_cast<uint32_t*>(wlist + kWarps * kChunk);
     uint32_t* cpre = cstart + 128;                                         // prefix over candidate cells
     uint32_t* cinv = cpre + 129;
-    uint32_t* vrank = cinv + 128;                                          // vertex list: rank
-    uint32_t* vid = vrank + a.vlist_cap;                                   // vertex list: grid vertex id
     __shared__ uint32_t s_nv, s_tot, s_wsum[4];
     const CandTables tabs{cstart, cpre, cinv};
 
@@ -211,12 +218,30 @@ __global__ void k_field_aniso_grouped(GroupArgs a, uint32_t ratio, const Counter
                 if (slot < a.vlist_cap) {
                     vid[slot] = v;
                     vrank[slot] = band_rank(a.band, v);
+                    vsum[slot] = 0.f;
                 }
             }
         }
         __syncthreads();
         const uint32_t nv = min(s_nv, a.vlist_cap);
         if (nv == 0) continue;
+        const uint32_t ntiles = (nv + 31) / 32;
+        auto vertex_pos = [&](uint32_t q) {
+            uint32_t x, y, z;
+            unlin3(vid[q], a.sc, x, y, z);
+            return make_float3(vpos1(x, a.sc.min[0], a.sc.cs), vpos1(y, a.sc.min[1], a.sc.cs),
+                               vpos1(z, a.sc.min[2], a.sc.cs));
+        };
+        for (uint32_t t = tid; t < ntiles; t += kBT) {
+            float4 l = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), h = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+            for (uint32_t q = 32 * t; q < min(nv, 32 * t + 32); ++q) {
+                const float3 v = vertex_pos(q);
+                l.x = fminf(l.x, v.x); l.y = fminf(l.y, v.y); l.z = fminf(l.z, v.z);
+                h.x = fmaxf(h.x, v.x); h.y = fmaxf(h.y, v.y); h.z = fmaxf(h.z, v.z);
+            }
+            tbox[2 * t] = l;
+            tbox[2 * t + 1] = h;
+        }
 
         // 2. candidate cells of the window
         const float b0[3] = {vpos1(lo[0], a.sc.min[0], a.sc.cs), vpos1(lo[1], a.sc.min[1], a.sc.cs),
@@ -225,92 +250,77 @@ __global__ void k_field_aniso_grouped(GroupArgs a, uint32_t ratio, const Counter
                              vpos1(hi[2] - 1, a.sc.min[2], a.sc.cs)};
         const uint32_t total = group_candidates(a.sp, a.ranges, a.invol, a.reach, c, b0, b1, tabs, s_wsum, &s_tot);
 
-        // 3. vertex passes; candidates streamed per pass
-        for (uint32_t vb = 0; vb < nv; vb += kBT) {
-            const bool have = vb + tid < nv;
-            uint32_t rank = 0;
-            float vx = 0.f, vy = 0.f, vz = 0.f;
-            if (have) {
-                rank = vrank[vb + tid];
-                uint32_t x, y, z;
-                unlin3(vid[vb + tid], a.sc, x, y, z);
-                vx = vpos1(x, a.sc.min[0], a.sc.cs);
-                vy = vpos1(y, a.sc.min[1], a.sc.cs);
-                vz = vpos1(z, a.sc.min[2], a.sc.cs);
-            }
-            // bounding box of this warp's vertices
-            float mnx = have ? vx : 3.0e38f, mny = have ? vy : 3.0e38f, mnz = have ? vz : 3.0e38f;
-            float mxx = have ? vx : -3.0e38f, mxy = have ? vy : -3.0e38f, mxz = have ? vz : -3.0e38f;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
-                mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
-                mnz = fminf(mnz, __shfl_xor_sync(0xffffffffu, mnz, o));
-                mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
-                mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
-                mxz = fmaxf(mxz, __shfl_xor_sync(0xffffffffu, mxz, o));
-            }
-            const bool warp_active = __any_sync(0xffffffffu, have);
-            float sum = 0.f;
-            for (uint32_t cb = 0; cb < total; cb += kChunk) {
-                // load one candidate record per thread
-                const uint32_t j = cb + tid;
+        // 3. candidates streamed once through shared memory; per chunk the
+        //    warps take the group's 32-vertex tiles round robin, each keeping
+        //    the candidates whose support reaches its tile's box
+        for (uint32_t cb = 0; cb < total; cb += kChunk) {
+            for (uint32_t q = tid; q < (uint32_t)kChunk; q += kBT) {
+                const uint32_t j = cb + q;
                 if (j < total) {
                     int cell;
                     const uint32_t i = candidate(j, tabs, &cell);
                     float4 r[4];
                     load_record(a.grec, a.smoothed, a.sigma, i, cinv[cell] != 0, r);
-                    float4* dst = rec + 4 * tid;
+                    float4* dst = rec + 4 * q;
                     dst[0] = r[0];
                     dst[1] = r[1];
                     dst[2] = r[2];
                     dst[3] = r[3];
                 }
-                __syncthreads();
-                const uint32_t cn = min((uint32_t)kChunk, total - cb);
-                if (warp_active) {
-                    // candidates whose support reaches this warp's vertex box
-                    uint32_t wc = 0;
-                    uint16_t* mylist = wlist + warp * kChunk;
-                    for (uint32_t q = 0; q < cn; q += 32) {
-                        const uint32_t idx = q + lane;
-                        bool keep = false;
-                        if (idx < cn) {
-                            const float4 r0 = rec[4 * idx];
-                            const float gx = fmaxf(0.f, fmaxf(mnx - r0.x, r0.x - mxx));
-                            const float gy = fmaxf(0.f, fmaxf(mny - r0.y, r0.y - mxy));
-                            const float gz = fmaxf(0.f, fmaxf(mnz - r0.z, r0.z - mxz));
-                            keep = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
-                        }
-                        const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                        if (keep) mylist[wc + __popc(m & ((1u << lane) - 1u))] = (uint16_t)idx;
-                        wc += __popc(m);
+            }
+            __syncthreads();
+            const uint32_t cn = min((uint32_t)kChunk, total - cb);
+            uint16_t* mylist = wlist + warp * kChunk;
+            for (uint32_t t = warp; t < ntiles; t += kWarps) {
+                const float4 tl = tbox[2 * t], th = tbox[2 * t + 1];
+                uint32_t wc = 0;
+                for (uint32_t q = 0; q < cn; q += 32) {
+                    const uint32_t idx = q + lane;
+                    bool keep = false;
+                    if (idx < cn) {
+                        const float4 r0 = rec[4 * idx];
+                        const float gx = fmaxf(0.f, fmaxf(tl.x - r0.x, r0.x - th.x));
+                        const float gy = fmaxf(0.f, fmaxf(tl.y - r0.y, r0.y - th.y));
+                        const float gz = fmaxf(0.f, fmaxf(tl.z - r0.z, r0.z - th.z));
+                        keep = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
                     }
-                    __syncwarp();
-                    if (have) {
-                        for (uint32_t k = 0; k < wc; ++k) {
-                            const float4* r = rec + 4 * mylist[k];
-                            const float4 r0 = r[0];
-                            const float rx = r0.x - vx, ry = r0.y - vy, rz = r0.z - vz;
-                            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                            if (d2 < r0.w) {
-                                const float4 g0 = r[1], g1 = r[2], g2 = r[3];
-                                const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
-                                const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
-                                const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
-                                const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
-                                if (q2 < 1.0f) {
-                                    const float u = 1.0f - q2;
-                                    sum = fmaf(g0.w, u * u * u, sum);
-                                }
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    if (keep) mylist[wc + __popc(m & ((1u << lane) - 1u))] = (uint16_t)idx;
+                    wc += __popc(m);
+                }
+                __syncwarp();
+                const uint32_t v = 32 * t + lane;
+                if (wc && v < nv) {
+                    const float3 vp = vertex_pos(v);
+                    float sum = vsum[v];
+                    for (uint32_t k = 0; k < wc; ++k) {
+                        const float4* r = rec + 4 * mylist[k];
+                        const float4 r0 = r[0];
+                        const float rx = r0.x - vp.x, ry = r0.y - vp.y, rz = r0.z - vp.z;
+                        const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                        if (d2 < r0.w) {
+                            const float4 g0 = r[1], g1 = r[2], g2 = r[3];
+                            const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
+                            const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
+                            const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
+                            const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+                            if (q2 < 1.0f) {
+                                const float u = 1.0f - q2;
+                                sum = fmaf(g0.w, u * u * u, sum);
                             }
                         }
                     }
+                    vsum[v] = sum;
                 }
-                __syncthreads();
+                __syncwarp();
             }
-            if (have && rank < nb) a.phi[rank] = sum - 0.5f;
+            __syncthreads();
         }
+        for (uint32_t v = tid; v < nv; v += kBT) {
+            const uint32_t rank = vrank[v];
+            if (rank < nb) a.phi[rank] = vsum[v] - 0.5f;
+        }
+        __syncthreads();
     }
 }
 
@@ -531,8 +541,9 @@ bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
 {
     // the group's index box is at most (ratio + 2)^3 vertices
     const uint32_t vcap = (ratio + 2) * (ratio + 2) * (ratio + 2);
-    const size_t smem = sizeof(float4) * 4 * kChunk + sizeof(uint16_t) * kWarps * kChunk +
-                        sizeof(uint32_t) * (128 + 129 + 128) + sizeof(uint32_t) * 2 * vcap;
+    const size_t smem = sizeof(float4) * 4 * kChunk + sizeof(float4) * 2 * ((vcap + 31) / 32) +
+                        3 * sizeof(uint32_t) * vcap + sizeof(uint16_t) * kWarps * kChunk +
+                        sizeof(uint32_t) * (128 + 129 + 128);
     if (smem > 200 * 1024) return false;
     static bool configured = false;
     if (!configured) {
