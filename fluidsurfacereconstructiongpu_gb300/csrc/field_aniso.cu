@@ -28,11 +28,6 @@ namespace {
 
 constexpr int kBT = 256;            // threads per block
 constexpr int kWarps = kBT / 32;
-#ifndef FSR_FIELD_CHUNK
-#define FSR_FIELD_CHUNK 128
-#endif
-constexpr int kChunk = FSR_FIELD_CHUNK;  // candidate records per shared-memory chunk (a multiple of 32)
-static_assert(kChunk % 32 == 0 && kChunk <= 65536, "chunk indices are 16-bit, warp lists step by 32");
 constexpr int kMaxCells = 125;      // 5 x 5 x 5 window
 
 struct GroupArgs {
@@ -171,156 +166,267 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ grec, con
     }
 }
 
-__global__ void k_field_aniso_grouped(GroupArgs a, uint32_t ratio, const Counters* ctr)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t ntile_cap = (a.vlist_cap + 31) / 32;
-    float4* rec = reinterpret_cast<float4*>(smem);                         // kChunk * 4 float4
-    float4* tbox = rec + 4 * kChunk;                                       // per 32-vertex tile: lo, hi
-    uint32_t* vid = reinterpret_cast<uint32_t*>(tbox + 2 * ntile_cap);     // vertex list: grid vertex id
-    uint32_t* vrank = vid + a.vlist_cap;                                   // vertex list: band rank
-    float* vsum = reinterpret_cast<float*>(vrank + a.vlist_cap);           // per vertex partial sum
-    uint16_t* wlist = reinterpret_cast<uint16_t*>(vsum + a.vlist_cap);     // kWarps * kChunk
-    uint32_t* cstart = reinterpret_cast<uint32_t*>(wlist + kWarps * kChunk);
-    uint32_t* cpre = cstart + 128;                                         // prefix over candidate cells
-    uint32_t* cinv = cpre + 129;
-    __shared__ uint32_t s_nv, s_tot, s_wsum[4];
-    const CandTables tabs{cstart, cpre, cinv};
+// ---------------------------------------------------------------- forward
+constexpr int kFT = 128;                 // threads per block of the forward kernel
+constexpr int kFWarps = kFT / 32;
+constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept in registers)
+constexpr int kPassVerts = 32 * kPassTiles;
 
+// Per-warp shared memory of the forward kernel.
+struct WarpSlice {
+    float4 rec[32 * 4];          // the current chunk's candidate records, one per lane
+    float4 vpos[kPassVerts];     // the pass's band vertices: position, band rank (bits)
+    float4 box[2 * kPassTiles];  // per tile: lo, hi
+    uint32_t cstart[128];
+    uint32_t cpre[kMaxCells + 1];
+    uint32_t cinv[128];
+};
+
+// Warp-level version of group_candidates: the same cells, the same order.
+__device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ranges,
+                                    const uint8_t* __restrict__ invol, const float* __restrict__ reach,
+                                    const int c[3], const float b0[3], const float b1[3], WarpSlice& w)
+{
+    const int lane = threadIdx.x & 31;
+    const int lx = clampi(c[0] - 2, 0, (int)sp.res[0] - 1), hx = clampi(c[0] + 2, 0, (int)sp.res[0] - 1);
+    const int ly = clampi(c[1] - 2, 0, (int)sp.res[1] - 1), hy = clampi(c[1] + 2, 0, (int)sp.res[1] - 1);
+    const int lz = clampi(c[2] - 2, 0, (int)sp.res[2] - 1), hz = clampi(c[2] + 2, 0, (int)sp.res[2] - 1);
+    uint32_t running = 0;
+    for (int k0 = 0; k0 < kMaxCells; k0 += 32) {
+        const int k = k0 + lane;
+        uint32_t cnt = 0, st = 0, inv = 0;
+        if (k < kMaxCells) {
+            const int xx = lx + k % 5, yy = ly + (k / 5) % 5, zz = lz + k / 25;
+            if (xx <= hx && yy <= hy && zz <= hz) {
+                const uint32_t cell = lin3(xx, yy, zz, sp);
+                const uint2 r = __ldg(&ranges[cell]);
+                if (r.x != kEmpty) {
+                    inv = __ldg(&invol[cell]);
+                    bool keep = true;
+                    if (inv) {
+                        const float cs = sp.cs;
+                        const float cx0 = sp.min[0] + xx * cs, cy0 = sp.min[1] + yy * cs, cz0 = sp.min[2] + zz * cs;
+                        const float gx = fmaxf(0.f, fmaxf(cx0 - b1[0], b0[0] - (cx0 + cs)));
+                        const float gy = fmaxf(0.f, fmaxf(cy0 - b1[1], b0[1] - (cy0 + cs)));
+                        const float gz = fmaxf(0.f, fmaxf(cz0 - b1[2], b0[2] - (cz0 + cs)));
+                        const float cr = cull_radius(__ldg(&reach[cell]), cs);
+                        keep = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < cr * cr;
+                    }
+                    if (keep) {
+                        st = r.x;
+                        cnt = r.y - r.x;
+                    }
+                }
+            }
+        }
+        uint32_t x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (k < kMaxCells) {
+            w.cstart[k] = st;
+            w.cinv[k] = inv;
+            w.cpre[k] = running + x - cnt;
+        }
+        running += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) w.cpre[kMaxCells] = running;
+    __syncwarp();
+    return running;
+}
+
+// (1 - q2)^3 and the coefficient of the record at r for vertex v; false
+// when v lies outside the support (q2 >= 1: the term is exactly zero).
+__device__ __forceinline__ bool term(const float4* r, float4 v, float& u3, float& coef)
+{
+    const float4 q0 = r[0], g0 = r[1], g1 = r[2], g2 = r[3];
+    const float rx = q0.x - v.x, ry = q0.y - v.y, rz = q0.z - v.z;
+    const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
+    const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
+    const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
+    const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+    const float u = 1.0f - q2;
+    u3 = u * u * u;
+    coef = g0.w;
+    return q2 < 1.0f;
+}
+
+__device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
+{
+    const float gx = fmaxf(0.f, fmaxf(lo.x - r0.x, r0.x - hi.x));
+    const float gy = fmaxf(0.f, fmaxf(lo.y - r0.y, r0.y - hi.y));
+    const float gz = fmaxf(0.f, fmaxf(lo.z - r0.z, r0.z - hi.z));
+    return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
+}
+
+// One warp per window group, groups handed out dynamically; no block-wide
+// barriers.  The warp walks the group's index box 32 vertices at a time and
+// collects up to 256 band vertices per pass (8 tiles of 32).  Per pass it
+// streams the window's candidates 32 at a time: each lane loads one
+// candidate's record into the warp's shared-memory slice once (candidates
+// that reach none of the pass's tiles are dropped first), then for every
+// tile the warp keeps the candidates whose support sphere reaches the
+// tile's box and each lane adds their terms for its vertex of that tile.
+// A vertex's sum takes the candidates in window order.
+__global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32_t ratio, Counters* ctr)
+{
+    __shared__ WarpSlice slices[kFWarps];
+    const int lane = threadIdx.x & 31;
+    WarpSlice& w = slices[threadIdx.x >> 5];
+    const CandTables tabs{w.cstart, w.cpre, w.cinv};
     const uint32_t nb = min(ctr->n_band, a.cap);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
 
-    for (uint32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(&ctr->work_field, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
         int c[3], lo[3], hi[3];
-        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;  // uniform across the block
+        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
         const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
         const int nbox = nx * ny * nz;
+        bool tables = false;
+        uint32_t total = 0;
 
-        // 1. the group's band vertices, in box order within each warp
-        if (tid == 0) s_nv = 0;
-        __syncthreads();
-        for (int base = 0; base < nbox; base += kBT) {
-            const int i = base + tid;
+        auto pass = [&](uint32_t nv) {
+            if (!tables) {
+                const float b0[3] = {vpos1(lo[0], a.sc.min[0], a.sc.cs), vpos1(lo[1], a.sc.min[1], a.sc.cs),
+                                     vpos1(lo[2], a.sc.min[2], a.sc.cs)};
+                const float b1[3] = {vpos1(hi[0] - 1, a.sc.min[0], a.sc.cs), vpos1(hi[1] - 1, a.sc.min[1], a.sc.cs),
+                                     vpos1(hi[2] - 1, a.sc.min[2], a.sc.cs)};
+                total = warp_candidates(a.sp, a.ranges, a.invol, a.reach, c, b0, b1, w);
+                tables = true;
+            }
+            const uint32_t ntiles = (nv + 31) / 32;
+            // tile boxes (lane t: tile t) and the pass's box
+            float4 pl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), ph = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+            if ((uint32_t)lane < ntiles) {
+                for (uint32_t q = 32 * lane; q < min(nv, 32 * lane + 32); ++q) {
+                    const float4 v = w.vpos[q];
+                    pl.x = fminf(pl.x, v.x); pl.y = fminf(pl.y, v.y); pl.z = fminf(pl.z, v.z);
+                    ph.x = fmaxf(ph.x, v.x); ph.y = fmaxf(ph.y, v.y); ph.z = fmaxf(ph.z, v.z);
+                }
+                w.box[2 * lane] = pl;
+                w.box[2 * lane + 1] = ph;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                pl.x = fminf(pl.x, __shfl_xor_sync(0xffffffffu, pl.x, o));
+                pl.y = fminf(pl.y, __shfl_xor_sync(0xffffffffu, pl.y, o));
+                pl.z = fminf(pl.z, __shfl_xor_sync(0xffffffffu, pl.z, o));
+                ph.x = fmaxf(ph.x, __shfl_xor_sync(0xffffffffu, ph.x, o));
+                ph.y = fmaxf(ph.y, __shfl_xor_sync(0xffffffffu, ph.y, o));
+                ph.z = fmaxf(ph.z, __shfl_xor_sync(0xffffffffu, ph.z, o));
+            }
+            __syncwarp();
+            float sum[kPassTiles];
+#pragma unroll
+            for (int t = 0; t < kPassTiles; ++t) sum[t] = 0.f;
+            for (uint32_t cb = 0; cb < total; cb += 32) {
+                const uint32_t j = cb + lane;
+                bool keep = false;
+                float4 r0 = make_float4(0.f, 0.f, 0.f, -1.f);
+                if (j < total) {
+                    int cell;
+                    const uint32_t i = candidate(j, tabs, &cell);
+                    const bool inv = w.cinv[cell] != 0;
+                    if (inv) {
+                        r0 = __ldg(a.grec + 4ull * i);
+                    } else {
+                        const float4 s = __ldg(&a.smoothed[i]);
+                        r0 = make_float4(s.x, s.y, s.z, 1.0f);
+                    }
+                    keep = reaches(r0, pl, ph);
+                    if (keep) {
+                        float4* dst = w.rec + 4 * lane;
+                        if (inv) {
+                            const float4* gsrc = a.grec + 4ull * i;
+                            dst[1] = __ldg(gsrc + 1);
+                            dst[2] = __ldg(gsrc + 2);
+                            dst[3] = __ldg(gsrc + 3);
+                        } else {
+                            dst[1] = make_float4(1.f, 0.f, 0.f, a.sigma * __ldg(&a.smoothed[i].w));
+                            dst[2] = make_float4(0.f, 1.f, 0.f, 0.f);
+                            dst[3] = make_float4(0.f, 0.f, 1.f, 0.f);
+                        }
+                    } else {
+                        r0.w = -1.f;  // reaches no tile
+                    }
+                    w.rec[4 * lane] = r0;
+                }
+                const uint32_t any = __ballot_sync(0xffffffffu, keep);
+                __syncwarp();
+                if (any) {
+#pragma unroll
+                    for (int t = 0; t < kPassTiles; ++t) {
+                        if ((uint32_t)t < ntiles) {
+                            const uint32_t m = __ballot_sync(0xffffffffu, keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]));
+                            const uint32_t v = 32 * t + lane;
+                            if (m && v < nv) {
+                                const float4 vp = w.vpos[v];
+                                float s = sum[t];
+                                // two kept candidates per step, evaluated without
+                                // branches; their terms enter the sum in order
+                                for (uint32_t mm = m; mm;) {
+                                    const int ka = __ffs(mm) - 1;
+                                    mm &= mm - 1u;
+                                    const bool two = mm != 0u;
+                                    const int kb = two ? __ffs(mm) - 1 : ka;
+                                    mm &= two ? mm - 1u : ~0u;
+                                    float ua, ub, ca, cb;
+                                    const bool ina = term(w.rec + 4 * ka, vp, ua, ca);
+                                    const bool inb = term(w.rec + 4 * kb, vp, ub, cb);
+                                    if (ina) s = fmaf(ca, ua, s);
+                                    if (two && inb) s = fmaf(cb, ub, s);
+                                }
+                                sum[t] = s;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+#pragma unroll
+            for (int t = 0; t < kPassTiles; ++t) {
+                const uint32_t v = 32 * t + lane;
+                if (v < nv) {
+                    const uint32_t rank = __float_as_uint(w.vpos[v].w);
+                    if (rank < nb) a.phi[rank] = sum[t] - 0.5f;
+                }
+            }
+            __syncwarp();
+        };
+
+        uint32_t count = 0;
+        for (int base = 0; base < nbox; base += 32) {
+            const int i = base + lane;
             bool in = false;
             uint32_t v = 0;
+            int lx = 0, ly = 0, lz = 0;
             if (i < nbox) {
-                const int lx = i % nx, ly = (i / nx) % ny, lz = i / (nx * ny);
+                lx = i % nx;
+                ly = (i / nx) % ny;
+                lz = i / (nx * ny);
                 v = lin3(lo[0] + lx, lo[1] + ly, lo[2] + lz, a.sc);
                 in = band_has(a.band, v);
             }
             const uint32_t m = __ballot_sync(0xffffffffu, in);
-            uint32_t off = 0;
-            if (lane == 0 && m) off = atomicAdd(&s_nv, __popc(m));
-            off = __shfl_sync(0xffffffffu, off, 0);
-            if (in) {
-                const uint32_t slot = off + __popc(m & ((1u << lane) - 1u));
-                if (slot < a.vlist_cap) {
-                    vid[slot] = v;
-                    vrank[slot] = band_rank(a.band, v);
-                    vsum[slot] = 0.f;
-                }
+            if (count + __popc(m) > (uint32_t)kPassVerts) {  // the pass is full: run it first
+                pass(count);
+                count = 0;
             }
+            if (in)
+                w.vpos[count + __popc(m & ((1u << lane) - 1u))] =
+                    make_float4(vpos1(lo[0] + lx, a.sc.min[0], a.sc.cs), vpos1(lo[1] + ly, a.sc.min[1], a.sc.cs),
+                                vpos1(lo[2] + lz, a.sc.min[2], a.sc.cs), __uint_as_float(band_rank(a.band, v)));
+            count += __popc(m);
+            __syncwarp();
         }
-        __syncthreads();
-        const uint32_t nv = min(s_nv, a.vlist_cap);
-        if (nv == 0) continue;
-        const uint32_t ntiles = (nv + 31) / 32;
-        auto vertex_pos = [&](uint32_t q) {
-            uint32_t x, y, z;
-            unlin3(vid[q], a.sc, x, y, z);
-            return make_float3(vpos1(x, a.sc.min[0], a.sc.cs), vpos1(y, a.sc.min[1], a.sc.cs),
-                               vpos1(z, a.sc.min[2], a.sc.cs));
-        };
-        for (uint32_t t = tid; t < ntiles; t += kBT) {
-            float4 l = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), h = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
-            for (uint32_t q = 32 * t; q < min(nv, 32 * t + 32); ++q) {
-                const float3 v = vertex_pos(q);
-                l.x = fminf(l.x, v.x); l.y = fminf(l.y, v.y); l.z = fminf(l.z, v.z);
-                h.x = fmaxf(h.x, v.x); h.y = fmaxf(h.y, v.y); h.z = fmaxf(h.z, v.z);
-            }
-            tbox[2 * t] = l;
-            tbox[2 * t + 1] = h;
-        }
-
-        // 2. candidate cells of the window
-        const float b0[3] = {vpos1(lo[0], a.sc.min[0], a.sc.cs), vpos1(lo[1], a.sc.min[1], a.sc.cs),
-                             vpos1(lo[2], a.sc.min[2], a.sc.cs)};
-        const float b1[3] = {vpos1(hi[0] - 1, a.sc.min[0], a.sc.cs), vpos1(hi[1] - 1, a.sc.min[1], a.sc.cs),
-                             vpos1(hi[2] - 1, a.sc.min[2], a.sc.cs)};
-        const uint32_t total = group_candidates(a.sp, a.ranges, a.invol, a.reach, c, b0, b1, tabs, s_wsum, &s_tot);
-
-        // 3. candidates streamed once through shared memory; per chunk the
-        //    warps take the group's 32-vertex tiles round robin, each keeping
-        //    the candidates whose support reaches its tile's box
-        for (uint32_t cb = 0; cb < total; cb += kChunk) {
-            for (uint32_t q = tid; q < (uint32_t)kChunk; q += kBT) {
-                const uint32_t j = cb + q;
-                if (j < total) {
-                    int cell;
-                    const uint32_t i = candidate(j, tabs, &cell);
-                    float4 r[4];
-                    load_record(a.grec, a.smoothed, a.sigma, i, cinv[cell] != 0, r);
-                    float4* dst = rec + 4 * q;
-                    dst[0] = r[0];
-                    dst[1] = r[1];
-                    dst[2] = r[2];
-                    dst[3] = r[3];
-                }
-            }
-            __syncthreads();
-            const uint32_t cn = min((uint32_t)kChunk, total - cb);
-            uint16_t* mylist = wlist + warp * kChunk;
-            for (uint32_t t = warp; t < ntiles; t += kWarps) {
-                const float4 tl = tbox[2 * t], th = tbox[2 * t + 1];
-                uint32_t wc = 0;
-                for (uint32_t q = 0; q < cn; q += 32) {
-                    const uint32_t idx = q + lane;
-                    bool keep = false;
-                    if (idx < cn) {
-                        const float4 r0 = rec[4 * idx];
-                        const float gx = fmaxf(0.f, fmaxf(tl.x - r0.x, r0.x - th.x));
-                        const float gy = fmaxf(0.f, fmaxf(tl.y - r0.y, r0.y - th.y));
-                        const float gz = fmaxf(0.f, fmaxf(tl.z - r0.z, r0.z - th.z));
-                        keep = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
-                    }
-                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
-                    if (keep) mylist[wc + __popc(m & ((1u << lane) - 1u))] = (uint16_t)idx;
-                    wc += __popc(m);
-                }
-                __syncwarp();
-                const uint32_t v = 32 * t + lane;
-                if (wc && v < nv) {
-                    const float3 vp = vertex_pos(v);
-                    float sum = vsum[v];
-                    for (uint32_t k = 0; k < wc; ++k) {
-                        const float4* r = rec + 4 * mylist[k];
-                        const float4 r0 = r[0];
-                        const float rx = r0.x - vp.x, ry = r0.y - vp.y, rz = r0.z - vp.z;
-                        const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                        if (d2 < r0.w) {
-                            const float4 g0 = r[1], g1 = r[2], g2 = r[3];
-                            const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
-                            const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
-                            const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
-                            const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
-                            if (q2 < 1.0f) {
-                                const float u = 1.0f - q2;
-                                sum = fmaf(g0.w, u * u * u, sum);
-                            }
-                        }
-                    }
-                    vsum[v] = sum;
-                }
-                __syncwarp();
-            }
-            __syncthreads();
-        }
-        for (uint32_t v = tid; v < nv; v += kBT) {
-            const uint32_t rank = vrank[v];
-            if (rank < nb) a.phi[rank] = vsum[v] - 0.5f;
-        }
-        __syncthreads();
+        if (count > 0) pass(count);
+        __syncwarp();
     }
 }
 
@@ -536,20 +642,9 @@ bool launch_field_aniso_backward_grouped(const KernelCtx& c, const AnisoBwdArgs&
     return true;
 }
 
-bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, const BandView& band, uint32_t ratio,
+void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, const BandView& band, uint32_t ratio,
                                 Counters* ctr)
 {
-    // the group's index box is at most (ratio + 2)^3 vertices
-    const uint32_t vcap = (ratio + 2) * (ratio + 2) * (ratio + 2);
-    const size_t smem = sizeof(float4) * 4 * kChunk + sizeof(float4) * 2 * ((vcap + 31) / 32) +
-                        3 * sizeof(uint32_t) * vcap + sizeof(uint16_t) * kWarps * kChunk +
-                        sizeof(uint32_t) * (128 + 129 + 128);
-    if (smem > 200 * 1024) return false;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(k_field_aniso_grouped, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        configured = true;
-    }
     GroupArgs a;
     a.sp = f.sp;
     a.sc = f.sc;
@@ -562,13 +657,12 @@ bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
     a.phi = f.phi;
     a.sigma = f.sigma;
     a.cap = f.cap;
-    a.vlist_cap = vcap;
+    a.vlist_cap = 0;
     const uint64_t groups = (uint64_t)(f.sp.res[0] + 1) * (f.sp.res[1] + 1) * (f.sp.res[2] + 1);
     const unsigned grid = (unsigned)std::min<uint64_t>(
-        groups, std::max<uint64_t>(1, (uint64_t)c.num_sms * 8 / std::max(1, c.grid_div)));
-    k_field_aniso_grouped<<<grid, kBT, smem, c.stream>>>(a, ratio, ctr);
+        (groups + kFWarps - 1) / kFWarps, std::max<uint64_t>(1, (uint64_t)c.num_sms * 16 / std::max(1, c.grid_div)));
+    k_field_aniso_grouped<<<grid, kFT, 0, c.stream>>>(a, ratio, ctr);
     ++g_launches;
-    return true;
 }
 
 }  // namespace fsr

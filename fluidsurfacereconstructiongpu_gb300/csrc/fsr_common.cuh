@@ -42,7 +42,9 @@ struct Counters {
     uint32_t need_band;      // sizes wanted when an overflow happened
     uint32_t need_valid;
     uint32_t need_mesh;
-    uint32_t pad[5];
+    uint32_t work_field;     // next window group of the anisotropic field (dynamic scheduling)
+    uint32_t work_adjoint;   // the same for its adjoint
+    uint32_t pad[3];
 };
 
 // Rank directory over the band bitset: rank(v) = number of band vertices

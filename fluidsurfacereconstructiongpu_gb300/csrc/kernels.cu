@@ -424,75 +424,6 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
     rec[3] = make_float4(G[6], G[7], G[8], 0.f);
 }
 
-// computationOfScalarFieldGrid (cu:830-906): +-2 cell window; particles of
-// involved cells use sigma det(G) (1 - |G r|^2)^3, all other particles the
-// unscaled sigma (1 - |r|^2)^3 (cuh:312-322), each times m / rho.
-__global__ void k_field_aniso(AnisoFieldArgs a, const Counters* ctr)
-{
-    const uint32_t nb = min(ctr->n_band, a.cap);
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
-        uint32_t x, y, z;
-        unlin3(a.sv[t], a.sc, x, y, z);
-        const float vx = vpos1(x, a.sc.min[0], a.sc.cs), vy = vpos1(y, a.sc.min[1], a.sc.cs),
-                    vz = vpos1(z, a.sc.min[2], a.sc.cs);
-        const Window w = window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
-                                cell1(vz, a.sp.min[2], a.sp.cs), 2, a.sp);
-        float sum = 0.f;
-        const float cs = a.sp.cs;
-        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz) {
-            const float bz0 = a.sp.min[2] + zz * cs;
-            const float gz = fmaxf(0.f, fmaxf(bz0 - vz, vz - (bz0 + cs)));
-            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-                const float by0 = a.sp.min[1] + yy * cs;
-                const float gy = fmaxf(0.f, fmaxf(by0 - vy, vy - (by0 + cs)));
-                const float gyz = fmaf(gy, gy, gz * gz);
-                for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx) {
-                    const uint32_t c = lin3(xx, yy, zz, a.sp);
-                    const uint2 r = __ldg(&a.ranges[c]);
-                    if (r.x == kEmpty) continue;
-                    if (__ldg(&a.invol[c])) {
-                        // skip the cell when the vertex lies beyond the reach
-                        // (support + smoothing shift) of all its particles:
-                        // every term is zero
-                        const float bx0 = a.sp.min[0] + xx * cs;
-                        const float gx = fmaxf(0.f, fmaxf(bx0 - vx, vx - (bx0 + cs)));
-                        const float cr = cull_radius(__ldg(&a.cell_rmax[c]), cs);
-                        if (fmaf(gx, gx, gyz) >= cr * cr) continue;
-                        for (uint32_t i = r.x; i < r.y; ++i) {
-                            const float4 r0 = __ldg(&a.grec[4ull * i]);
-                            const float rx = r0.x - vx, ry = r0.y - vy, rz = r0.z - vz;
-                            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                            if (d2 >= r0.w) continue;
-                            const float4 g0 = __ldg(&a.grec[4ull * i + 1]);
-                            const float4 g1 = __ldg(&a.grec[4ull * i + 2]);
-                            const float4 g2 = __ldg(&a.grec[4ull * i + 3]);
-                            const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
-                            const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
-                            const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
-                            const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
-                            if (q2 < 1.0f) {
-                                const float u = 1.0f - q2;
-                                sum = fmaf(g0.w, u * u * u, sum);
-                            }
-                        }
-                    } else {
-                        for (uint32_t i = r.x; i < r.y; ++i) {
-                            const float4 s = __ldg(&a.smoothed[i]);
-                            const float rx = s.x - vx, ry = s.y - vy, rz = s.z - vz;
-                            const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
-                            if (d2 < 1.0f) {
-                                const float u = 1.0f - d2;
-                                sum = fmaf(a.sigma * s.w, u * u * u, sum);
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        a.phi[t] = sum - 0.5f;
-    }
-}
-
 // ------------------------------------------------------------ marching cubes
 __device__ __forceinline__ float field_at(const McArgs& a, int x, int y, int z)
 {
@@ -746,12 +677,6 @@ void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr)
 {
     if (!a.n) return;
     k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
-    ++g_launches;
-}
-
-void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr)
-{
-    k_field_aniso<<<persistent_blocks(c, a.cap, 16), kThreads, 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
 

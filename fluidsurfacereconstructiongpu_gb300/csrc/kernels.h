@@ -90,10 +90,8 @@ struct AnisoFieldArgs {
     float sigma;
     uint32_t cap;
 };
-void launch_field_aniso(const KernelCtx& c, const AnisoFieldArgs& a, Counters* ctr);
-// Window-grouped evaluation with shared-memory candidate staging; returns
-// false (nothing launched) when the grid ratio makes a group too large.
-bool launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& a, const BandView& band, uint32_t ratio,
+// computationOfScalarFieldGrid (cu:830-906), grouped by window (field_aniso.cu).
+void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& a, const BandView& band, uint32_t ratio,
                                 Counters* ctr);
 
 // Adjoint of the anisotropic field, grouped like the forward pass: adds

@@ -366,8 +366,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.phi = phi;
         fa.sigma = ca.sigma;
         fa.cap = h->cap_band;
-        if (!launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr))
-            launch_field_aniso(kc, fa, ctr);
+        launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr);
     } else {
         mark(5);
         mark(6);
