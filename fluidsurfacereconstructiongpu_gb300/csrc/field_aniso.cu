@@ -287,7 +287,6 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
         const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
-        const int nbox = nx * ny * nz;
         bool tables = false;
         uint32_t total = 0;
 
@@ -400,32 +399,53 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             __syncwarp();
         };
 
-        uint32_t count = 0;
-        for (int base = 0; base < nbox; base += 32) {
-            const int i = base + lane;
-            bool in = false;
-            uint32_t v = 0;
-            int lx = 0, ly = 0, lz = 0;
-            if (i < nbox) {
-                lx = i % nx;
-                ly = (i / nx) % ny;
-                lz = i / (nx * ny);
-                v = lin3(lo[0] + lx, lo[1] + ly, lo[2] + lz, a.sc);
-                in = band_has(a.band, v);
+        // band vertices of the box by row segments of at most 32 vertices (two
+        // bitset words), `per` segments per step so that one step adds at most
+        // kPassVerts vertices; a pass runs whenever the next step would not fit
+        const int nseg = (nx + 31) / 32;
+        const int units = ny * nz * nseg;
+        const int per = max(1, min(32, kPassVerts / min(nx, 32)));
+        int ub = 0;
+        while (ub < units) {
+            uint32_t count = 0;
+            for (; ub < units; ub += per) {
+                const int u = ub + lane;
+                uint32_t rm = 0, v0 = 0;
+                int x0 = 0, ry = 0, rz = 0;
+                if (lane < per && u < units) {
+                    const int seg = u % nseg, row = u / nseg;
+                    x0 = lo[0] + 32 * seg;
+                    const int wd = min(32, hi[0] - x0);
+                    ry = lo[1] + row % ny;
+                    rz = lo[2] + row / ny;
+                    v0 = lin3(x0, ry, rz, a.sc);
+                    const uint32_t w0 = v0 >> 5, sh = v0 & 31u;
+                    uint64_t bits = __ldg(a.band.bits + w0);
+                    if (sh + (uint32_t)wd > 32u) bits |= (uint64_t)__ldg(a.band.bits + w0 + 1) << 32;
+                    rm = (uint32_t)(bits >> sh) & (wd >= 32 ? 0xffffffffu : ((1u << wd) - 1u));
+                }
+                const uint32_t n = __popc(rm);
+                uint32_t x = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                const uint32_t tot = __shfl_sync(0xffffffffu, x, 31);
+                // (tot <= kPassVerts by the choice of `per`: an empty pass always takes the step)
+                if (count > 0 && count + tot > (uint32_t)kPassVerts) break;  // run the pass, then this step again
+                uint32_t slot = count + x - n;
+                for (uint32_t m = rm; m; m &= m - 1u) {
+                    const int bx = __ffs(m) - 1;
+                    w.vpos[slot++] = make_float4(vpos1(x0 + bx, a.sc.min[0], a.sc.cs), vpos1(ry, a.sc.min[1], a.sc.cs),
+                                                 vpos1(rz, a.sc.min[2], a.sc.cs),
+                                                 __uint_as_float(band_rank(a.band, v0 + (uint32_t)bx)));
+                }
+                count += tot;
             }
-            const uint32_t m = __ballot_sync(0xffffffffu, in);
-            if (count + __popc(m) > (uint32_t)kPassVerts) {  // the pass is full: run it first
-                pass(count);
-                count = 0;
-            }
-            if (in)
-                w.vpos[count + __popc(m & ((1u << lane) - 1u))] =
-                    make_float4(vpos1(lo[0] + lx, a.sc.min[0], a.sc.cs), vpos1(lo[1] + ly, a.sc.min[1], a.sc.cs),
-                                vpos1(lo[2] + lz, a.sc.min[2], a.sc.cs), __uint_as_float(band_rank(a.band, v)));
-            count += __popc(m);
             __syncwarp();
+            if (count > 0) pass(count);
         }
-        if (count > 0) pass(count);
         __syncwarp();
     }
 }
