@@ -4,6 +4,7 @@
 #include "cov_solver.cuh"
 
 #include <algorithm>
+#include <cmath>
 
 namespace fsr {
 
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
 // reference's order with the reference's roundings.  smoothed.w = m / rho.
 __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
-                                                     float one_minus_lambda, float lambda, float mass,
+                                                     float R_lt2, float one_minus_lambda, float lambda, float mass,
                                                      float4* __restrict__ mean, float4* __restrict__ smoothed)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -340,12 +341,11 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
             }
             for (uint32_t i = beg; i < end; ++i) {
                 const float4 q = __ldg(&sorted[i]);
-                const float d = __fsqrt_rn(dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z)));
-                float wt = 0.f;
-                if (d < R) {
-                    const float s = __fdiv_rn(d, R);
-                    wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
-                }
+                const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+                // d >= R: weight 0, and +0 terms leave the sums unchanged
+                if (!(d2 < R_lt2)) continue;
+                const float s = __fdiv_rn(__fsqrt_rn(d2), R);
+                const float wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
                 ws = __fadd_rn(ws, wt);
                 mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
                 my = __fadd_rn(my, __fmul_rn(q.y, wt));
@@ -400,9 +400,10 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
             for (uint32_t i = beg; i < end; ++i) {
                 const float4 q = __ldg(&a.sorted[i]);
                 const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
-                const float d = __fsqrt_rn(dot3_rn(vx, vy, vz));
-                if (d <= a.R) ++nn;
-                if (d < a.R) acc.add(vx, vy, vz, d, a.R);
+                const float d2 = dot3_rn(vx, vy, vz);
+                if (!(d2 < a.R_le2)) continue;  // d > R: neither counted nor weighed
+                ++nn;
+                if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
             }
         }
     float G[9];
@@ -598,6 +599,23 @@ __global__ void k_particle_flags(const uint32_t* __restrict__ skeys, const uint8
 
 // ------------------------------------------------------------ launchers
 
+// Smallest float x >= 0 whose correctly rounded square root is >= R
+// (strict = false) or > R (strict = true): for d2 >= 0,
+//   sqrt_rn(d2) <  R  <=>  d2 < threshold(R, false)
+//   sqrt_rn(d2) <= R  <=>  d2 < threshold(R, true)
+// so the kernels test distances without a square root and take the root
+// only where the weight needs it.  sqrtf on the host and __fsqrt_rn on the
+// device are both the IEEE correctly rounded square root.
+static float sqrt_threshold(float R, bool strict)
+{
+    auto ok = [&](float x) { return strict ? std::sqrt(x) > R : std::sqrt(x) >= R; };
+    float x = R * R;
+    if (!(x > 0.0f) || !std::isfinite(x)) return x;
+    while (x > 0.0f && ok(std::nextafterf(x, 0.0f))) x = std::nextafterf(x, 0.0f);
+    while (!ok(x)) x = std::nextafterf(x, INFINITY);
+    return x;
+}
+
 void launch_hash(const KernelCtx& c, const float* xyz, uint32_t n, const Grid& sp, uint32_t* keys,
                  uint32_t* vals, Counters* ctr)
 {
@@ -669,13 +687,17 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     if (!n) return;
     // (1.0 - lambda) is evaluated in double and rounded (cu:656)
     const float oml = (float)(1.0 - (double)lambda);
-    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, oml, lambda, mass, mean, smoothed);
+    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), oml, lambda,
+                                                       mass, mean, smoothed);
     ++g_launches;
 }
 
-void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr)
+void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
 {
-    if (!a.n) return;
+    if (!a0.n) return;
+    CovArgs a = a0;
+    a.R_lt2 = sqrt_threshold(a.R, false);
+    a.R_le2 = sqrt_threshold(a.R, true);
     k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
     ++g_launches;
 }

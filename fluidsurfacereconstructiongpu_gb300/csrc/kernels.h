@@ -74,6 +74,7 @@ struct CovArgs {
     uint32_t n;
     float R, h, h2, h_inv, mass, sigma;
     uint32_t min_neighbors;
+    float R_lt2, R_le2;  // squared-distance thresholds of d < R and d <= R (set by launch_cov)
 };
 void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr);
 
