@@ -420,9 +420,13 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= f.n) return;
-    const bool act = f.invol[f.skeys[t]] != 0;
     float4 gmo = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (act) {
+    const float4 gr0 = a.gG[3ull * t], gr1 = a.gG[3ull * t + 1], gr2 = a.gG[3ull * t + 2];
+    const float gG[9] = {gr0.x, gr0.y, gr0.z, gr1.x, gr1.y, gr1.z, gr2.x, gr2.y, gr2.z};
+    bool any = false;
+    for (int k = 0; k < 9; ++k) any = any || gG[k] != 0.f;
+    // only involved particles with a non-zero dL/dG have work
+    if (any && f.invol[f.skeys[t]] != 0) {
         const float4 p = f.sorted[t];
         const float4 m = f.mean[t];
         const Window w = narrow(window(cell1(p.x, f.sp.min[0], f.sp.cs), cell1(p.y, f.sp.min[1], f.sp.cs),
@@ -445,8 +449,9 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
                     for (uint32_t i = beg; i < end; ++i) {
                         const float4 q = __ldg(&f.sorted[i]);
                         const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
-                        const float d = __fsqrt_rn(dot3_rn(vx, vy, vz));
-                        fn(i, vx, vy, vz, d);
+                        const float d2 = dot3_rn(vx, vy, vz);
+                        if (!(d2 < f.R_le2)) continue;  // d > R: no part in either pass
+                        fn(i, vx, vy, vz, __fsqrt_rn(d2));
                     }
                 }
         };
@@ -454,11 +459,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
             if (d <= f.R) ++nn;
             if (d < f.R) acc.add(vx, vy, vz, d, f.R);
         });
-        const float4 gr0 = a.gG[3ull * t], gr1 = a.gG[3ull * t + 1], gr2 = a.gG[3ull * t + 2];
-        const float gG[9] = {gr0.x, gr0.y, gr0.z, gr1.x, gr1.y, gr1.z, gr2.x, gr2.y, gr2.z};
-        bool any = false;
-        for (int k = 0; k < 9; ++k) any = any || gG[k] != 0.f;
-        if (nn >= f.min_neighbors && any) {
+        if (nn >= f.min_neighbors) {
             const float W = acc.wsum.s, iw = 1.0f / W;
             float C[3][3] = {{(f.h2 + acc.c11.s) * iw, acc.c12.s * iw, acc.c13.s * iw},
                              {acc.c12.s * iw, (f.h2 + acc.c22.s) * iw, acc.c23.s * iw},

@@ -134,6 +134,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
         ca.mass = h->hdr_last.particle_mass;
         ca.sigma = a.sigma;
         ca.min_neighbors = p.min_neighbors;
+        ca.R_lt2 = sqrt_threshold(R, false);
+        ca.R_le2 = sqrt_threshold(R, true);
     }
     const KernelCtx kc{st, h->num_sms};
     const bool want_radius = grad_particle_radius && (p.method == FSR_METHOD_ZB05 || p.method == FSR_METHOD_AKINCI12);

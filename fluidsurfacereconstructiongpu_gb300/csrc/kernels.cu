@@ -606,7 +606,7 @@ __global__ void k_particle_flags(const uint32_t* __restrict__ skeys, const uint8
 // so the kernels test distances without a square root and take the root
 // only where the weight needs it.  sqrtf on the host and __fsqrt_rn on the
 // device are both the IEEE correctly rounded square root.
-static float sqrt_threshold(float R, bool strict)
+float sqrt_threshold(float R, bool strict)
 {
     auto ok = [&](float x) { return strict ? std::sqrt(x) > R : std::sqrt(x) >= R; };
     float x = R * R;

@@ -61,6 +61,11 @@ void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counte
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
                    float R, float lambda, float mass, float4* mean, float4* smoothed);
 
+// Smallest float x whose correctly rounded square root is >= R (> R when
+// strict): sqrt_rn(d2) < R <=> d2 < sqrt_threshold(R, false) and
+// sqrt_rn(d2) <= R <=> d2 < sqrt_threshold(R, true).
+float sqrt_threshold(float R, bool strict);
+
 struct CovArgs {
     Grid sp;
     const float4* sorted;
