@@ -31,6 +31,10 @@ WORKLOADS = {
     # the anisotropic 1M frame (headline)
     "aniso1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="yu13", smoothing_lambda=0.9,
                     aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
+    # 8M particles: the 32^3-lattice generator at r = 0.002 (200^3 lattice, a 0.4 cube), anisotropic
+    # field with the 1M frame's settings (grid spacing 0.5r: a 1020^3 scalar grid, 1.06e9 vertices)
+    "aniso8m": dict(kind="lattice", n_side=200, r=0.002, seed=1, method="yu13", smoothing_lambda=0.9,
+                    aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
     # the anisotropic frame at 2^18 particles (profiling captures)
     "aniso256k": dict(kind="dam_break", n=1 << 18, r=0.004, seed=2, method="yu13", smoothing_lambda=0.9,
                       aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
@@ -303,7 +307,7 @@ def main():
 
     # CPU baseline first (rank 0, N = 1), before any GPU work
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and fr.n <= (1 << 21):
         s, label, threads, sample = cpu_frame(w, fr, args.cpu_field_stride)
         cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample}
 
@@ -429,9 +433,10 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded dam-break, L2 flushed between steps)",
+            "vs_baseline": None, "dtype": "f32", "data": f"synthetic ({fr.name}, seeded; L2 flushed between steps)",
             "config": {"workload": args.workload, "particles": fr.n, "method": w["method"],
                        "band_vertices": B, "triangles": int(st.n_mesh_vertices) // 3,
+                       "device_bytes": int(rec.stats().device_bytes), "fp64_fallbacks": int(st.n_fp64_fallbacks),
                        "scalar_grid": list(st.scalar_res), "l2": "flushed (256 MB write) between steps",
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": fr.n / e2e_step, "unit": "particles/s", "h2d_bytes_per_step": h2d,

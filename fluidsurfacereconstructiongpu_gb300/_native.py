@@ -52,7 +52,7 @@ class Stats(ctypes.Structure):
                 ("n_valid_cubes", c_u64), ("n_mesh_vertices", c_u64), ("spatial_res", c_u32 * 3),
                 ("scalar_res", c_u32 * 3), ("n_fp64_fallbacks", c_u32), ("n_retries", c_u32),
                 ("n_kernel_launches", c_u32), ("n_backward_launches", c_u32),
-                ("stage_ms", c_f32 * NUM_STAGES), ("total_ms", c_f32)]
+                ("stage_ms", c_f32 * NUM_STAGES), ("total_ms", c_f32), ("device_bytes", c_u64)]
 
 
 class FsrError(RuntimeError):

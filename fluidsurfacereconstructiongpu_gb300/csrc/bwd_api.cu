@@ -145,6 +145,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
                         want_radius ? (float*)h->gscalar.ptr : nullptr, d_grad_xyz);
     BCK(cudaGetLastError());
     h->stats.n_backward_launches = (uint32_t)(g_launches - launches0);
+    h->stats.device_bytes = 0;
+    for (DevBuf* b : h->all_buffers()) h->stats.device_bytes += b->bytes;
     if (grad_particle_radius) {
         float r = 0.f;
         if (want_radius) {

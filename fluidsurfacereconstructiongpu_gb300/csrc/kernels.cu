@@ -316,8 +316,9 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
 // reference's order with the reference's roundings.  smoothed.w = m / rho.
 __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
-                                                     float R_lt2, float one_minus_lambda, float lambda, float mass,
-                                                     float4* __restrict__ mean, float4* __restrict__ smoothed)
+                                                     float R_lt2, float one_minus_lambda, float lambda,
+                                                     float mass, float4* __restrict__ mean,
+                                                     float4* __restrict__ smoothed)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -397,14 +398,30 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
                     end = max(end, r.y);
                 }
             }
-            for (uint32_t i = beg; i < end; ++i) {
-                const float4 q = __ldg(&a.sorted[i]);
+            // d > R: neither counted nor weighed; four candidates per step
+            auto take = [&](const float4& q) {
                 const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
                 const float d2 = dot3_rn(vx, vy, vz);
-                if (!(d2 < a.R_le2)) continue;  // d > R: neither counted nor weighed
-                ++nn;
-                if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
+                if (d2 < a.R_le2) {
+                    ++nn;
+                    if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
+                }
+            };
+            auto dist2 = [&](const float4& q) {
+                return dot3_rn(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), __fsub_rn(q.z, m.z));
+            };
+            uint32_t i = beg;
+            for (; i + 4 <= end; i += 4) {
+                const float4 q0 = __ldg(&a.sorted[i]), q1 = __ldg(&a.sorted[i + 1]);
+                const float4 q2 = __ldg(&a.sorted[i + 2]), q3 = __ldg(&a.sorted[i + 3]);
+                const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
+                const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
+                if (n0) take(q0);
+                if (n1) take(q1);
+                if (n2) take(q2);
+                if (n3) take(q3);
             }
+            for (; i < end; ++i) take(__ldg(&a.sorted[i]));
         }
     float G[9];
     const float rmax = covariance_to_G(acc, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
@@ -687,8 +704,8 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     if (!n) return;
     // (1.0 - lambda) is evaluated in double and rounded (cu:656)
     const float oml = (float)(1.0 - (double)lambda);
-    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), oml, lambda,
-                                                       mass, mean, smoothed);
+    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), oml,
+                                                       lambda, mass, mean, smoothed);
     ++g_launches;
 }
 

@@ -453,6 +453,8 @@ fsr_status frame_finish(fsr_handle* h, const FramePlan& fp, bool timing, bool* r
     s.n_fp64_fallbacks = hc.n_fp64;
     s.n_kernel_launches = h->launches_frame;
     s.n_backward_launches = 0;
+    s.device_bytes = 0;
+    for (DevBuf* b : h->all_buffers()) s.device_bytes += b->bytes;
     for (int a = 0; a < 3; ++a) {
         s.spatial_res[a] = fp.sp.res[a];
         s.scalar_res[a] = fp.sc.res[a];

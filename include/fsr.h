@@ -100,6 +100,7 @@ typedef struct fsr_stats {
     uint32_t n_backward_launches;  /* kernels launched by the last fsr_backward call */
     float stage_ms[FSR_NUM_STAGES];/* with FSR_FLAG_STAGE_TIMING */
     float total_ms;
+    uint64_t device_bytes;         /* device memory held by the handle's pools */
 } fsr_stats;
 
 typedef struct fsr_handle fsr_handle;
