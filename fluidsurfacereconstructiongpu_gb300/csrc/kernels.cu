@@ -138,7 +138,7 @@ __global__ void k_involved_cells(Grid sp, const uint8_t* __restrict__ occ, const
 // taken in the reference's order with the reference's roundings (FP64 where
 // the source promotes).
 __global__ void k_colorfield(const float4* __restrict__ sorted, uint32_t n, const uint2* __restrict__ ranges,
-                             Grid sp, float h, double k_spiky, float mass, uint8_t* __restrict__ psurf)
+                             Grid sp, float h, float h_lt2, double k_spiky, float mass, uint8_t* __restrict__ psurf)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -147,33 +147,40 @@ __global__ void k_colorfield(const float4* __restrict__ sorted, uint32_t n, cons
                             cell1(p.z, sp.min[2], sp.cs), 1, sp);
     uint32_t nn = 0;
     float sx = 0.f, sy = 0.f, sz = 0.f;
+    // the particles of a row of x-adjacent cells are contiguous in sorted order
     for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy)
-            for (int xx = w.lo[0]; xx <= w.hi[0]; ++xx) {
-                const uint2 r = ranges[lin3(xx, yy, zz, sp)];
-                if (r.x == kEmpty) continue;
-                for (uint32_t i = r.x; i < r.y; ++i) {
-                    const float4 q = sorted[i];
-                    float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
-                    const float d2 = dot3_rn(rx, ry, rz);
-                    if (!(d2 > 0.0f)) continue;
-                    ++nn;
-                    const float d = __fsqrt_rn(d2);
-                    float grad = 0.0f;
-                    if (!(d >= h)) {
-                        const float x = __double2float_rn(__dsub_rn(1.0, (double)__fdiv_rn(d, h)));
-                        grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, (double)x), (double)x));
-                    }
-                    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(d2));
-                    rx = __fmul_rn(rx, inv);
-                    ry = __fmul_rn(ry, inv);
-                    rz = __fmul_rn(rz, inv);
-                    const float coef = __fmul_rn(__fdiv_rn(mass, q.w), grad);
-                    sx = __fadd_rn(sx, __fmul_rn(coef, rx));
-                    sy = __fadd_rn(sy, __fmul_rn(coef, ry));
-                    sz = __fadd_rn(sz, __fmul_rn(coef, rz));
+        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+            const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
+            uint32_t beg = kEmpty, end = 0;
+            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                const uint2 r = __ldg(&ranges[c0 + xx]);
+                if (r.x != kEmpty) {
+                    beg = min(beg, r.x);
+                    end = max(end, r.y);
                 }
             }
+            for (uint32_t i = beg; i < end; ++i) {
+                const float4 q = __ldg(&sorted[i]);
+                float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
+                const float d2 = dot3_rn(rx, ry, rz);
+                if (!(d2 > 0.0f)) continue;
+                ++nn;
+                // d >= h: the gradient is 0 and the +0 / -0 terms leave the
+                // sums (never -0) unchanged
+                if (!(d2 < h_lt2)) continue;
+                const float d = __fsqrt_rn(d2);
+                const float x = __double2float_rn(__dsub_rn(1.0, (double)__fdiv_rn(d, h)));
+                const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, (double)x), (double)x));
+                const float inv = __fdiv_rn(1.0f, d);
+                rx = __fmul_rn(rx, inv);
+                ry = __fmul_rn(ry, inv);
+                rz = __fmul_rn(rz, inv);
+                const float coef = __fmul_rn(__fdiv_rn(mass, q.w), grad);
+                sx = __fadd_rn(sx, __fmul_rn(coef, rx));
+                sy = __fadd_rn(sy, __fmul_rn(coef, ry));
+                sz = __fadd_rn(sz, __fmul_rn(coef, rz));
+            }
+        }
     const bool s = nn < 25u || __fsqrt_rn(dot3_rn(sx, sy, sz)) > 3.0f;
     psurf[t] = s ? 1 : 0;
 }
@@ -670,7 +677,8 @@ void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, con
     if (!n) return;
     // -45 / (pi h^4) exactly as the reference evaluates it in double
     const double k = -45.0 / (3.1415926535 * (double)h2 * (double)h2);
-    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, h, k, mass, psurf);
+    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, h, sqrt_threshold(h, false), k, mass,
+                                                           psurf);
     ++g_launches;
 }
 
