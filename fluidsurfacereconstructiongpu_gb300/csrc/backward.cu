@@ -31,14 +31,6 @@ namespace {
 
 constexpr int kT = 256;
 
-__device__ __forceinline__ void atomic_add3(float4* p, float x, float y, float z)
-{
-    float* f = reinterpret_cast<float*>(p);
-    atomicAdd(f, x);
-    atomicAdd(f + 1, y);
-    atomicAdd(f + 2, z);
-}
-
 // ---------------------------------------------------------------- MC
 __global__ void k_mc_backward(BwdArgs a, const Counters* ctr)
 {
@@ -503,7 +495,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
                 // d w / d v = -3 d v / R^3
                 const float kw = (vAv + gW) * (-3.0f * d * invR3);
                 const float gx = 2.f * wt * Avx + kw * vx, gy = 2.f * wt * Avy + kw * vy, gz = 2.f * wt * Avz + kw * vz;
-                atomic_add3(a.gx + i, gx, gy, gz);
+                atomicAdd(a.gx + i, make_float4(gx, gy, gz, 0.f));
                 gmx -= gx;
                 gmy -= gy;
                 gmz -= gz;
@@ -516,7 +508,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
 
 // ---------------------------------------------------------------- smoothing
 __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4* mean, const uint2* ranges, Grid sp,
-                                  uint32_t n, float R, float lambda)
+                                  uint32_t n, float R, float R_lt2, float lambda)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -526,55 +518,49 @@ __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4*
     float gix = (1.0f - lambda) * gs.x, giy = (1.0f - lambda) * gs.y, giz = (1.0f - lambda) * gs.z;
     if (gmx != 0.f || gmy != 0.f || gmz != 0.f) {
         const float4 p = sorted[t];
-        const float4 m = mean[t];
+        const float4 m = mean[t];  // m.w: the forward's weight sum W
         const Window w = narrow(window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
                                        cell1(p.z, sp.min[2], sp.cs), 2, sp),
                                 p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
-        // weight sum, then the neighbour gradients
-        float W = 0.f;
-        for (int pass = 0; pass < 2; ++pass) {
-            const float iw = pass ? 1.0f / W : 0.f;
-            const float gnx = gmx * iw, gny = gmy * iw, gnz = gmz * iw;
-            for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-                for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-                    const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
-                    uint32_t beg = kEmpty, end = 0;
-                    for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                        const uint2 r = __ldg(&ranges[c0 + xx]);
-                        if (r.x != kEmpty) {
-                            beg = min(beg, r.x);
-                            end = max(end, r.y);
-                        }
-                    }
-                    for (uint32_t i = beg; i < end; ++i) {
-                        const float4 q = __ldg(&sorted[i]);
-                        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                        const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-                        if (!(d < R)) continue;
-                        const float s = d / R;
-                        const float wt = 1.0f - s * s * s;
-                        if (!pass) {
-                            W += wt;
-                            continue;
-                        }
-                        // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
-                        const float gw = gnx * (q.x - m.x) + gny * (q.y - m.y) + gnz * (q.z - m.z);
-                        float ex = 0.f, ey = 0.f, ez = 0.f;
-                        if (d > 0.f) {
-                            const float k = gw * (-3.0f * s * s / R) / d;  // dw/dd * (x_i - x_j)/d
-                            ex = k * dx;
-                            ey = k * dy;
-                            ez = k * dz;
-                        }
-                        gix += ex;
-                        giy += ey;
-                        giz += ez;
-                        atomic_add3(a.gx + i, wt * gnx - ex, wt * gny - ey, wt * gnz - ez);
+        const float iw = 1.0f / m.w;
+        const float gnx = gmx * iw, gny = gmy * iw, gnz = gmz * iw;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
+                uint32_t beg = kEmpty, end = 0;
+                for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                    const uint2 r = __ldg(&ranges[c0 + xx]);
+                    if (r.x != kEmpty) {
+                        beg = min(beg, r.x);
+                        end = max(end, r.y);
                     }
                 }
-        }
+                for (uint32_t i = beg; i < end; ++i) {
+                    const float4 q = __ldg(&sorted[i]);
+                    // the forward's neighbour decision, exactly
+                    const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+                    if (!(d2 < R_lt2)) continue;
+                    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                    const float d = sqrtf(d2);
+                    const float s = d / R;
+                    const float wt = 1.0f - s * s * s;
+                    // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
+                    const float gw = gnx * (q.x - m.x) + gny * (q.y - m.y) + gnz * (q.z - m.z);
+                    float ex = 0.f, ey = 0.f, ez = 0.f;
+                    if (d > 0.f) {
+                        const float k = gw * (-3.0f * s * s / R) / d;  // dw/dd * (x_i - x_j)/d
+                        ex = k * dx;
+                        ey = k * dy;
+                        ez = k * dz;
+                    }
+                    gix += ex;
+                    giy += ey;
+                    giz += ez;
+                    atomicAdd(a.gx + i, make_float4(wt * gnx - ex, wt * gny - ey, wt * gnz - ez, 0.f));
+                }
+            }
     }
-    atomic_add3(a.gx + t, gix, giy, giz);
+    atomicAdd(a.gx + t, make_float4(gix, giy, giz, 0.f));
 }
 
 __global__ void k_unsort(const float4* gx, const uint32_t* perm, uint32_t n, float* out)
@@ -625,7 +611,7 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
         }
         k_cov_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, *cov);
         k_smooth_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, cov->sorted, cov->mean, cov->ranges, cov->sp, a.n, R,
-                                                           lambda);
+                                                           cov->R_lt2, lambda);
         g_launches += 3;
     } else if (method == FSR_METHOD_TC01) {
         k_field_backward_iso<true><<<nblk(a.n), kT, 0, c.stream>>>(a);

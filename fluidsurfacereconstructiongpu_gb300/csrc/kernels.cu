@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
     mx = __fdiv_rn(mx, ws);
     my = __fdiv_rn(my, ws);
     mz = __fdiv_rn(mz, ws);
-    mean[t] = make_float4(mx, my, mz, 0.f);
+    mean[t] = make_float4(mx, my, mz, ws);  // w: the weight sum (the adjoint divides by it)
     smoothed[t] = make_float4(__fadd_rn(__fmul_rn(one_minus_lambda, p.x), __fmul_rn(lambda, mx)),
                               __fadd_rn(__fmul_rn(one_minus_lambda, p.y), __fmul_rn(lambda, my)),
                               __fadd_rn(__fmul_rn(one_minus_lambda, p.z), __fmul_rn(lambda, mz)),
