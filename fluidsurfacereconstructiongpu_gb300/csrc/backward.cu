@@ -424,8 +424,6 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
         const Window w = narrow(window(cell1(p.x, f.sp.min[0], f.sp.cs), cell1(p.y, f.sp.min[1], f.sp.cs),
                                        cell1(p.z, f.sp.min[2], f.sp.cs), 2, f.sp),
                                 m.x, m.y, m.z, cull_radius(f.R, f.sp.cs), f.sp);
-        CovAccum acc;
-        uint32_t nn = 0;
         auto each = [&](auto&& fn) {
             for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
                 for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
@@ -447,15 +445,12 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
                     }
                 }
         };
-        each([&](uint32_t, float vx, float vy, float vz, float d) {
-            if (d <= f.R) ++nn;
-            if (d < f.R) acc.add(vx, vy, vz, d, f.R);
-        });
-        if (nn >= f.min_neighbors) {
-            const float W = acc.wsum.s, iw = 1.0f / W;
-            float C[3][3] = {{(f.h2 + acc.c11.s) * iw, acc.c12.s * iw, acc.c13.s * iw},
-                             {acc.c12.s * iw, (f.h2 + acc.c22.s) * iw, acc.c23.s * iw},
-                             {acc.c13.s * iw, acc.c23.s * iw, (f.h2 + acc.c33.s) * iw}};
+        // the forward's normalised covariance and weight sum (k_cov); flag 0:
+        // too few neighbours, G did not depend on them
+        const float4 c0 = f.crec[2ull * t], c1 = f.crec[2ull * t + 1];
+        if (c1.w != 0.f) {
+            const float W = c1.z, iw = 1.0f / W;
+            float C[3][3] = {{c0.x, c0.y, c0.z}, {c0.y, c0.w, c1.x}, {c0.z, c1.x, c1.y}};
             float C0[3][3];
             for (int i = 0; i < 3; ++i)
                 for (int k = 0; k < 3; ++k) C0[i][k] = C[i][k];

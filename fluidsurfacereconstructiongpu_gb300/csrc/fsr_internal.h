@@ -64,6 +64,7 @@ struct fsr_handle {
     fsr::DevBuf sorted;                  // float4 x,y,z,density in cell order
     fsr::DevBuf psurf;                   // Akinci12 per-particle surface flags
     fsr::DevBuf mean, smoothed, grec;    // Yu13
+    fsr::DevBuf covrec;                  // Yu13: normalised covariance, weight sum, neighbour-count flag
     fsr::DevBuf pflags;                  // u32 surface flags (debug)
     // cell-sized
     fsr::DevBuf ranges, occ, surf, invol, cell_rmax;

@@ -432,6 +432,12 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
         }
     float G[9];
     const float rmax = covariance_to_G(acc, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
+    if (a.crec) {  // the normalised covariance for the adjoint (the same expressions as covariance_to_G)
+        const bool used = nn >= a.min_neighbors;
+        const float iw = used ? 1.0f / acc.wsum.s : 0.f;
+        a.crec[2ull * t] = make_float4((a.h2 + acc.c11.s) * iw, acc.c12.s * iw, acc.c13.s * iw, (a.h2 + acc.c22.s) * iw);
+        a.crec[2ull * t + 1] = make_float4(acc.c23.s * iw, (a.h2 + acc.c33.s) * iw, acc.wsum.s, used ? 1.f : 0.f);
+    }
     const float det = G[0] * G[4] * G[8] + G[1] * G[5] * G[6] + G[2] * G[3] * G[7] - G[0] * G[5] * G[7] -
                       G[1] * G[3] * G[8] - G[2] * G[4] * G[6];
     const float4 sm = a.smoothed[t];

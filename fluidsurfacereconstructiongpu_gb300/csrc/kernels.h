@@ -75,6 +75,7 @@ struct CovArgs {
     const uint32_t* skeys;
     const uint8_t* invol;
     float4* grec;  // 4 float4 per particle: (x,y,z smoothed, r2max) (G rows, coef in row 0's w)
+    float4* crec;  // 2 float4 per particle: (C00 C01 C02 C11) (C12 C22 W, 1 if C was used else 0)
     float* cell_rmax;  // per cell: largest support radius + smoothing shift of its particles (zeroed per frame)
     uint32_t n;
     float R, h, h2, h_inv, mass, sigma;

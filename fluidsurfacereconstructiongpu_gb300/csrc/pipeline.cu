@@ -173,7 +173,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &mesh_pos, &mesh_nrm, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -233,6 +233,7 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         CK(h->mean.ensure(16ull * nn));
         CK(h->smoothed.ensure(16ull * nn));
         CK(h->grec.ensure(64ull * nn));
+        CK(h->covrec.ensure(32ull * nn));
     }
     if (p.method == FSR_METHOD_AKINCI12) CK(h->psurf.ensure(nn));
     if (keep) CK(h->pflags.ensure(4ull * nn));
@@ -342,6 +343,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         ca.skeys = skeys;
         ca.invol = (const uint8_t*)h->invol.ptr;
         ca.grec = (float4*)h->grec.ptr;
+        ca.crec = (float4*)h->covrec.ptr;
         ca.cell_rmax = (float*)h->cell_rmax.ptr;
         ca.n = n;
         ca.R = R;
