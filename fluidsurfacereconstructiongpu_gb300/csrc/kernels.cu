@@ -323,43 +323,83 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
 // reference's order with the reference's roundings.  smoothed.w = m / rho.
 __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
-                                                     float R_lt2, float one_minus_lambda, float lambda,
-                                                     float mass, float4* __restrict__ mean,
+                                                     float R_lt2, int coop_ok, float one_minus_lambda,
+                                                     float lambda, float mass, float4* __restrict__ mean,
                                                      float4* __restrict__ smoothed)
 {
+    __shared__ float4 s_q[kThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const float4 p = sorted[t];
+    const bool active = t < n;
+    if (__all_sync(0xffffffffu, !active)) return;
+    const int lane = threadIdx.x & 31;
+    float4* sq = s_q + (threadIdx.x & ~31u);
+    const float4 p = active ? sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
     // cells beyond R on some axis only hold zero-weight particles, whose +0
     // terms leave the exact sums unchanged: skip them
     const Window w = narrow(window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
                                    cell1(p.z, sp.min[2], sp.cs), 2, sp),
                             p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
     float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
-    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-            const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
-            uint32_t beg = kEmpty, end = 0;
-            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                const uint2 r = __ldg(&ranges[c0 + xx]);
-                if (r.x != kEmpty) {
-                    beg = min(beg, r.x);
-                    end = max(end, r.y);
-                }
-            }
-            for (uint32_t i = beg; i < end; ++i) {
-                const float4 q = __ldg(&sorted[i]);
-                const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
-                // d >= R: weight 0, and +0 terms leave the sums unchanged
-                if (!(d2 < R_lt2)) continue;
-                const float s = __fdiv_rn(__fsqrt_rn(d2), R);
-                const float wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
-                ws = __fadd_rn(ws, wt);
-                mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
-                my = __fadd_rn(my, __fmul_rn(q.y, wt));
-                mz = __fadd_rn(mz, __fmul_rn(q.z, wt));
+    auto add = [&](const float4& q) {
+        const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+        if (!(d2 < R_lt2)) return;  // d >= R: weight 0, and +0 terms leave the sums unchanged
+        const float s = __fdiv_rn(__fsqrt_rn(d2), R);
+        const float wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
+        ws = __fadd_rn(ws, wt);
+        mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
+        my = __fadd_rn(my, __fmul_rn(q.y, wt));
+        mz = __fadd_rn(mz, __fmul_rn(q.z, wt));
+    };
+    auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
+        const uint32_t c0 = lin3(x0, yy, zz, sp);
+        beg = kEmpty;
+        end = 0;
+        for (int xx = 0; xx <= x1 - x0; ++xx) {
+            const uint2 r = __ldg(&ranges[c0 + xx]);
+            if (r.x != kEmpty) {
+                beg = min(beg, r.x);
+                end = max(end, r.y);
             }
         }
+    };
+    // A warp whose windows span at most 4 cells per axis walks their union
+    // together: each chunk of 32 candidates is loaded once (one per lane)
+    // and every lane tests all of them, so no lane idles on a window of its
+    // own.  Exact: a candidate outside a lane's window lies beyond the cull
+    // radius of its particle on some axis (coop_ok: that radius is below 2
+    // cells, so the +-2 cell window never cuts a lane's narrowed window),
+    // and the lane's own candidates keep their window order.
+    int ulo[3], uhi[3];
+    bool compact = coop_ok != 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ulo[a] = (int)__reduce_min_sync(0xffffffffu, active ? (unsigned)w.lo[a] : 0x7fffffffu);
+        uhi[a] = (int)__reduce_max_sync(0xffffffffu, active ? (unsigned)(w.hi[a] + 1) : 0u) - 1;
+        compact = compact && uhi[a] - ulo[a] <= 3;
+    }
+    if (compact) {
+        for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
+            for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(ulo[0], uhi[0], yy, zz, beg, end);
+                for (uint32_t base = beg; base < end; base += 32) {
+                    if (base + lane < end) sq[lane] = __ldg(&sorted[base + lane]);
+                    __syncwarp();
+                    const uint32_t cnt = min(32u, end - base);
+                    for (uint32_t k = 0; k < cnt; ++k) add(sq[k]);
+                    __syncwarp();
+                }
+            }
+    } else {
+        if (!active) return;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
+                for (uint32_t i = beg; i < end; ++i) add(__ldg(&sorted[i]));
+            }
+    }
+    if (!active) return;
     // ws >= 1: the particle itself has weight 1
     mx = __fdiv_rn(mx, ws);
     my = __fdiv_rn(my, ws);
@@ -718,8 +758,11 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     if (!n) return;
     // (1.0 - lambda) is evaluated in double and rounded (cu:656)
     const float oml = (float)(1.0 - (double)lambda);
-    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), oml,
-                                                       lambda, mass, mean, smoothed);
+    // warps may walk the union of their windows when the cull radius stays
+    // below two cells (see k_smooth)
+    const int coop_ok = (R * 1.0001f + 1e-4f * sp.cs) < 2.0f * sp.cs * 0.9999f ? 1 : 0;
+    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), coop_ok,
+                                                       oml, lambda, mass, mean, smoothed);
     ++g_launches;
 }
 
