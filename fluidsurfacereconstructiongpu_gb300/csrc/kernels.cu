@@ -420,12 +420,15 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
 // (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
 __global__ void k_cov(CovArgs a, Counters* ctr)
 {
+    __shared__ float4 s_q[kThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = t < a.n && a.invol[a.skeys[t]];
     warp_count(&ctr->n_involved, act);
-    if (!act) return;
-    const float4 p = a.sorted[t];
-    const float4 m = a.mean[t];
+    if (__all_sync(0xffffffffu, !act)) return;
+    const int lane = threadIdx.x & 31;
+    float4* sq = s_q + (threadIdx.x & ~31u);
+    const float4 p = act ? a.sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
+    const float4 m = act ? a.mean[t] : p;
     // the window is centred on the particle's cell (cu:710-716); only
     // particles within R of the mean count or weigh, so cells beyond R of the
     // mean on some axis are skipped
@@ -434,42 +437,88 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
                             m.x, m.y, m.z, cull_radius(a.R, a.sp.cs), a.sp);
     CovAccum acc;
     uint32_t nn = 0;
-    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-            const uint32_t c0 = lin3(w.lo[0], yy, zz, a.sp);
-            uint32_t beg = kEmpty, end = 0;
-            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                const uint2 r = __ldg(&a.ranges[c0 + xx]);
-                if (r.x != kEmpty) {
-                    beg = min(beg, r.x);
-                    end = max(end, r.y);
-                }
-            }
-            // d > R: neither counted nor weighed; four candidates per step
-            auto take = [&](const float4& q) {
-                const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
-                const float d2 = dot3_rn(vx, vy, vz);
-                if (d2 < a.R_le2) {
-                    ++nn;
-                    if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
-                }
-            };
-            auto dist2 = [&](const float4& q) {
-                return dot3_rn(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), __fsub_rn(q.z, m.z));
-            };
-            uint32_t i = beg;
-            for (; i + 4 <= end; i += 4) {
-                const float4 q0 = __ldg(&a.sorted[i]), q1 = __ldg(&a.sorted[i + 1]);
-                const float4 q2 = __ldg(&a.sorted[i + 2]), q3 = __ldg(&a.sorted[i + 3]);
-                const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
-                const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
-                if (n0) take(q0);
-                if (n1) take(q1);
-                if (n2) take(q2);
-                if (n3) take(q3);
-            }
-            for (; i < end; ++i) take(__ldg(&a.sorted[i]));
+    // d > R: neither counted nor weighed
+    auto take = [&](const float4& q) {
+        const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
+        const float d2 = dot3_rn(vx, vy, vz);
+        if (d2 < a.R_le2) {
+            ++nn;
+            if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
         }
+    };
+    auto dist2 = [&](const float4& q) {
+        return dot3_rn(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), __fsub_rn(q.z, m.z));
+    };
+    auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
+        const uint32_t c0 = lin3(x0, yy, zz, a.sp);
+        beg = kEmpty;
+        end = 0;
+        for (int xx = 0; xx <= x1 - x0; ++xx) {
+            const uint2 r = __ldg(&a.ranges[c0 + xx]);
+            if (r.x != kEmpty) {
+                beg = min(beg, r.x);
+                end = max(end, r.y);
+            }
+        }
+    };
+    // Compact warps walk the union of their windows with staged candidates,
+    // as in k_smooth.  Exact when the +-2 cell window never cuts a lane's
+    // window narrowed about its mean (the mean lies within R of the particle:
+    // launch_cov checks R + cull radius < 2 cells), so every candidate the
+    // union adds lies beyond R of that lane's mean.
+    int ulo[3], uhi[3];
+    bool compact = a.coop_ok != 0;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        ulo[ax] = (int)__reduce_min_sync(0xffffffffu, act ? (unsigned)w.lo[ax] : 0x7fffffffu);
+        uhi[ax] = (int)__reduce_max_sync(0xffffffffu, act ? (unsigned)(w.hi[ax] + 1) : 0u) - 1;
+        compact = compact && uhi[ax] - ulo[ax] <= 3;
+    }
+    if (compact) {
+        for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
+            for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(ulo[0], uhi[0], yy, zz, beg, end);
+                for (uint32_t base = beg; base < end; base += 32) {
+                    if (base + lane < end) sq[lane] = __ldg(&a.sorted[base + lane]);
+                    __syncwarp();
+                    const uint32_t cnt = min(32u, end - base);
+                    uint32_t k = 0;
+                    for (; k + 4 <= cnt; k += 4) {
+                        const float4 q0 = sq[k], q1 = sq[k + 1], q2 = sq[k + 2], q3 = sq[k + 3];
+                        const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
+                        const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
+                        if (n0) take(q0);
+                        if (n1) take(q1);
+                        if (n2) take(q2);
+                        if (n3) take(q3);
+                    }
+                    for (; k < cnt; ++k) take(sq[k]);
+                    __syncwarp();
+                }
+            }
+        if (!act) return;
+    } else {
+        if (!act) return;
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
+                // four candidates per step
+                uint32_t i = beg;
+                for (; i + 4 <= end; i += 4) {
+                    const float4 q0 = __ldg(&a.sorted[i]), q1 = __ldg(&a.sorted[i + 1]);
+                    const float4 q2 = __ldg(&a.sorted[i + 2]), q3 = __ldg(&a.sorted[i + 3]);
+                    const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
+                    const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
+                    if (n0) take(q0);
+                    if (n1) take(q1);
+                    if (n2) take(q2);
+                    if (n3) take(q3);
+                }
+                for (; i < end; ++i) take(__ldg(&a.sorted[i]));
+            }
+    }
     float G[9];
     const float rmax = covariance_to_G(acc, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
     if (a.crec) {  // the normalised covariance for the adjoint (the same expressions as covariance_to_G)
@@ -772,6 +821,7 @@ void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
     CovArgs a = a0;
     a.R_lt2 = sqrt_threshold(a.R, false);
     a.R_le2 = sqrt_threshold(a.R, true);
+    a.coop_ok = (a.R + a.R * 1.0001f + 1e-4f * a.sp.cs) < 2.0f * a.sp.cs * 0.9999f ? 1 : 0;
     k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
