@@ -169,8 +169,12 @@ __global__ void k_colorfield(const float4* __restrict__ sorted, uint32_t n, cons
                 // sums (never -0) unchanged
                 if (!(d2 < h_lt2)) continue;
                 const float d = __fsqrt_rn(d2);
-                const float x = __double2float_rn(__dsub_rn(1.0, (double)__fdiv_rn(d, h)));
-                const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, (double)x), (double)x));
+                // x = float(1.0 - (double)(d / h)): the double difference of 1
+                // and a float is exact, so rounding it to float is the
+                // correctly rounded FP32 difference (no FP64 work needed)
+                const float x = __fsub_rn(1.0f, __fdiv_rn(d, h));
+                const double xd = (double)x;
+                const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, xd), xd));
                 const float inv = __fdiv_rn(1.0f, d);
                 rx = __fmul_rn(rx, inv);
                 ry = __fmul_rn(ry, inv);
