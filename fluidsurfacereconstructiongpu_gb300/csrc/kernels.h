@@ -48,6 +48,7 @@ void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* 
 struct IsoFieldArgs {
     Grid sp, sc;
     const float4* sorted;
+    const uint32_t* skeys;  // cell of each sorted particle
     const uint2* ranges;
     const uint32_t* sv;
     float* phi;

@@ -376,6 +376,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.sp = sp;
         fa.sc = sc;
         fa.sorted = sorted;
+        fa.skeys = skeys;
         fa.ranges = ranges;
         fa.sv = sv;
         fa.phi = phi;
