@@ -408,154 +408,202 @@ __device__ void g_to_c(const T V[3][3], const T l[3], float h_inv, const float g
         }
 }
 
+// Calls fn(i, q) for the sorted particles of each lane's cell window (rows of
+// x-adjacent cells merged).  Every lane of the warp calls it; lanes with
+// active = false take no particles.  A warp whose active windows span at
+// most 4 cells per axis walks their union together, 32 particles staged in
+// sq at a time (one load per particle for the whole warp); the caller sets
+// coop only when every particle the union adds fails each lane's own range
+// test, so each lane still sees exactly the particles that matter to it.
+template <class Fn>
+__device__ __forceinline__ void walk_windows(const Window& w, bool active, bool coop, const Grid& sp,
+                                             const uint2* __restrict__ ranges, const float4* __restrict__ sorted,
+                                             float4* sq, Fn fn)
+{
+    const int lane = threadIdx.x & 31;
+    auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
+        const uint32_t c0 = lin3(x0, yy, zz, sp);
+        beg = kEmpty;
+        end = 0;
+        for (int xx = 0; xx <= x1 - x0; ++xx) {
+            const uint2 r = __ldg(&ranges[c0 + xx]);
+            if (r.x != kEmpty) {
+                beg = min(beg, r.x);
+                end = max(end, r.y);
+            }
+        }
+    };
+    int ulo[3], uhi[3];
+    bool compact = coop;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        ulo[a] = (int)__reduce_min_sync(0xffffffffu, active ? (unsigned)w.lo[a] : 0x7fffffffu);
+        uhi[a] = (int)__reduce_max_sync(0xffffffffu, active ? (unsigned)(w.hi[a] + 1) : 0u) - 1;
+        compact = compact && uhi[a] - ulo[a] <= 3;
+    }
+    if (compact) {
+        for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
+            for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(ulo[0], uhi[0], yy, zz, beg, end);
+                for (uint32_t b = beg; b < end; b += 32) {
+                    if (b + lane < end) sq[lane] = __ldg(&sorted[b + lane]);
+                    __syncwarp();
+                    const uint32_t cnt = min(32u, end - b);
+                    if (active)
+                        for (uint32_t k = 0; k < cnt; ++k) fn(b + k, sq[k]);
+                    __syncwarp();
+                }
+            }
+    } else if (active) {
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
+                for (uint32_t i = beg; i < end; ++i) fn(i, __ldg(&sorted[i]));
+            }
+    }
+}
+
 __global__ void k_cov_backward(BwdArgs a, CovArgs f)
 {
+    __shared__ float4 s_q[kT];  // 32 staged particles per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= f.n) return;
+    const bool valid = t < f.n;
     float4 gmo = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 gr0 = a.gG[3ull * t], gr1 = a.gG[3ull * t + 1], gr2 = a.gG[3ull * t + 2];
-    const float gG[9] = {gr0.x, gr0.y, gr0.z, gr1.x, gr1.y, gr1.z, gr2.x, gr2.y, gr2.z};
-    bool any = false;
-    for (int k = 0; k < 9; ++k) any = any || gG[k] != 0.f;
-    // only involved particles with a non-zero dL/dG have work
-    if (any && f.invol[f.skeys[t]] != 0) {
-        const float4 p = f.sorted[t];
-        const float4 m = f.mean[t];
-        const Window w = narrow(window(cell1(p.x, f.sp.min[0], f.sp.cs), cell1(p.y, f.sp.min[1], f.sp.cs),
-                                       cell1(p.z, f.sp.min[2], f.sp.cs), 2, f.sp),
-                                m.x, m.y, m.z, cull_radius(f.R, f.sp.cs), f.sp);
-        auto each = [&](auto&& fn) {
-            for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-                for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-                    const uint32_t c0 = lin3(w.lo[0], yy, zz, f.sp);
-                    uint32_t beg = kEmpty, end = 0;
-                    for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                        const uint2 r = __ldg(&f.ranges[c0 + xx]);
-                        if (r.x != kEmpty) {
-                            beg = min(beg, r.x);
-                            end = max(end, r.y);
-                        }
-                    }
-                    for (uint32_t i = beg; i < end; ++i) {
-                        const float4 q = __ldg(&f.sorted[i]);
-                        const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
-                        const float d2 = dot3_rn(vx, vy, vz);
-                        if (!(d2 < f.R_le2)) continue;  // d > R: no part in either pass
-                        fn(i, vx, vy, vz, __fsqrt_rn(d2));
-                    }
-                }
-        };
-        // the forward's normalised covariance and weight sum (k_cov); flag 0:
-        // too few neighbours, G did not depend on them
-        const float4 c0 = f.crec[2ull * t], c1 = f.crec[2ull * t + 1];
-        if (c1.w != 0.f) {
-            const float W = c1.z, iw = 1.0f / W;
-            float C[3][3] = {{c0.x, c0.y, c0.z}, {c0.y, c0.w, c1.x}, {c0.z, c1.x, c1.y}};
-            float C0[3][3];
-            for (int i = 0; i < 3; ++i)
-                for (int k = 0; k < 3; ++k) C0[i][k] = C[i][k];
-            float lv[3], V[3][3], gC[3][3];
-            sym_eig3<float>(C, lv, V);
-            const float smax = fmaxf(fabsf(lv[0]), fmaxf(fabsf(lv[1]), fabsf(lv[2])));
-            const float smin = fminf(fabsf(lv[0]), fminf(fabsf(lv[1]), fabsf(lv[2])));
-            if (!(smin > 0.f) || smax > 1e4f * smin) {
-                double Cd[3][3], ld[3], Vd[3][3], gCd[3][3];
-                for (int i = 0; i < 3; ++i)
-                    for (int k = 0; k < 3; ++k) Cd[i][k] = C0[i][k];
-                sym_eig3<double>(Cd, ld, Vd);
-                g_to_c<double>(Vd, ld, f.h_inv, gG, gCd);
-                for (int i = 0; i < 3; ++i)
-                    for (int k = 0; k < 3; ++k) gC[i][k] = (float)gCd[i][k];
-            } else {
-                g_to_c<float>(V, lv, f.h_inv, gG, gC);
-            }
-            // C = A / W: dL/dA = gC / W, dL/dW = -<gC, C> / W
-            float gW = 0.f;
-            for (int i = 0; i < 3; ++i)
-                for (int k = 0; k < 3; ++k) gW -= gC[i][k] * C0[i][k];
-            gW *= iw;
-            float gA[3][3];
-            for (int i = 0; i < 3; ++i)
-                for (int k = 0; k < 3; ++k) gA[i][k] = gC[i][k] * iw;
-            const float R = f.R, invR3 = 1.0f / (R * R * R);
-            float gmx = 0.f, gmy = 0.f, gmz = 0.f;
-            each([&](uint32_t i, float vx, float vy, float vz, float d) {
-                if (!(d < R)) return;
-                const float s = d / R;
-                const float wt = 1.0f - s * s * s;
-                const float Avx = gA[0][0] * vx + gA[0][1] * vy + gA[0][2] * vz;
-                const float Avy = gA[1][0] * vx + gA[1][1] * vy + gA[1][2] * vz;
-                const float Avz = gA[2][0] * vx + gA[2][1] * vy + gA[2][2] * vz;
-                const float vAv = vx * Avx + vy * Avy + vz * Avz;
-                // d w / d v = -3 d v / R^3
-                const float kw = (vAv + gW) * (-3.0f * d * invR3);
-                const float gx = 2.f * wt * Avx + kw * vx, gy = 2.f * wt * Avy + kw * vy, gz = 2.f * wt * Avz + kw * vz;
-                atomicAdd(a.gx + i, make_float4(gx, gy, gz, 0.f));
-                gmx -= gx;
-                gmy -= gy;
-                gmz -= gz;
-            });
-            gmo = make_float4(gmx, gmy, gmz, 0.f);
+    float gG[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool act = false;
+    float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+    if (valid) {
+        const float4 gr0 = a.gG[3ull * t], gr1 = a.gG[3ull * t + 1], gr2 = a.gG[3ull * t + 2];
+        const float g9[9] = {gr0.x, gr0.y, gr0.z, gr1.x, gr1.y, gr1.z, gr2.x, gr2.y, gr2.z};
+        bool any = false;
+        for (int k = 0; k < 9; ++k) {
+            gG[k] = g9[k];
+            any = any || g9[k] != 0.f;
+        }
+        // only involved particles with a non-zero dL/dG whose G used their
+        // covariance have work; the forward kept the normalised covariance and
+        // its weight sum (k_cov; flag 0: too few neighbours)
+        if (any && f.invol[f.skeys[t]] != 0) {
+            c0 = f.crec[2ull * t];
+            c1 = f.crec[2ull * t + 1];
+            act = c1.w != 0.f;
         }
     }
-    a.gmean[t] = gmo;
+    if (__all_sync(0xffffffffu, !act)) {
+        if (valid) a.gmean[t] = gmo;
+        return;
+    }
+    const float4 p = act ? f.sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
+    const float4 m = act ? f.mean[t] : p;
+    const Window w = narrow(window(cell1(p.x, f.sp.min[0], f.sp.cs), cell1(p.y, f.sp.min[1], f.sp.cs),
+                                   cell1(p.z, f.sp.min[2], f.sp.cs), 2, f.sp),
+                            m.x, m.y, m.z, cull_radius(f.R, f.sp.cs), f.sp);
+    float gA[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float gW = 0.f;
+    if (act) {
+        const float W = c1.z, iw = 1.0f / W;
+        float C[3][3] = {{c0.x, c0.y, c0.z}, {c0.y, c0.w, c1.x}, {c0.z, c1.x, c1.y}};
+        float C0[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) C0[i][k] = C[i][k];
+        float lv[3], V[3][3], gC[3][3];
+        sym_eig3<float>(C, lv, V);
+        const float smax = fmaxf(fabsf(lv[0]), fmaxf(fabsf(lv[1]), fabsf(lv[2])));
+        const float smin = fminf(fabsf(lv[0]), fminf(fabsf(lv[1]), fabsf(lv[2])));
+        if (!(smin > 0.f) || smax > 1e4f * smin) {
+            double Cd[3][3], ld[3], Vd[3][3], gCd[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int k = 0; k < 3; ++k) Cd[i][k] = C0[i][k];
+            sym_eig3<double>(Cd, ld, Vd);
+            g_to_c<double>(Vd, ld, f.h_inv, gG, gCd);
+            for (int i = 0; i < 3; ++i)
+                for (int k = 0; k < 3; ++k) gC[i][k] = (float)gCd[i][k];
+        } else {
+            g_to_c<float>(V, lv, f.h_inv, gG, gC);
+        }
+        // C = A / W: dL/dA = gC / W, dL/dW = -<gC, C> / W
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) gW -= gC[i][k] * C0[i][k];
+        gW *= iw;
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) gA[i][k] = gC[i][k] * iw;
+    }
+    const float R = f.R, invR3 = 1.0f / (R * R * R);
+    float gmx = 0.f, gmy = 0.f, gmz = 0.f;
+    walk_windows(w, act, f.coop_ok != 0, f.sp, f.ranges, f.sorted, s_q + (threadIdx.x & ~31u),
+                 [&](uint32_t i, const float4& q) {
+        const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
+        const float d2 = dot3_rn(vx, vy, vz);
+        if (!(d2 < f.R_lt2)) return;  // the forward's weight test (d < R), exactly
+        const float d = __fsqrt_rn(d2);
+        const float s = d / R;
+        const float wt = 1.0f - s * s * s;
+        const float Avx = gA[0][0] * vx + gA[0][1] * vy + gA[0][2] * vz;
+        const float Avy = gA[1][0] * vx + gA[1][1] * vy + gA[1][2] * vz;
+        const float Avz = gA[2][0] * vx + gA[2][1] * vy + gA[2][2] * vz;
+        const float vAv = vx * Avx + vy * Avy + vz * Avz;
+        // d w / d v = -3 d v / R^3
+        const float kw = (vAv + gW) * (-3.0f * d * invR3);
+        const float gx = 2.f * wt * Avx + kw * vx, gy = 2.f * wt * Avy + kw * vy, gz = 2.f * wt * Avz + kw * vz;
+        atomicAdd(a.gx + i, make_float4(gx, gy, gz, 0.f));
+        gmx -= gx;
+        gmy -= gy;
+        gmz -= gz;
+    });
+    if (act) gmo = make_float4(gmx, gmy, gmz, 0.f);
+    if (valid) a.gmean[t] = gmo;
 }
 
 // ---------------------------------------------------------------- smoothing
 __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4* mean, const uint2* ranges, Grid sp,
-                                  uint32_t n, float R, float R_lt2, float lambda)
+                                  uint32_t n, float R, float R_lt2, int coop_ok, float lambda)
 {
+    __shared__ float4 s_q[kT];  // 32 staged particles per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const float4 gs = a.gsmooth[t];
-    const float4 gmc = a.gmean[t];
+    const bool valid = t < n;
+    float4 gs = make_float4(0.f, 0.f, 0.f, 0.f), gmc = gs;
+    if (valid) {
+        gs = a.gsmooth[t];
+        gmc = a.gmean[t];
+    }
     const float gmx = lambda * gs.x + gmc.x, gmy = lambda * gs.y + gmc.y, gmz = lambda * gs.z + gmc.z;
     float gix = (1.0f - lambda) * gs.x, giy = (1.0f - lambda) * gs.y, giz = (1.0f - lambda) * gs.z;
-    if (gmx != 0.f || gmy != 0.f || gmz != 0.f) {
-        const float4 p = sorted[t];
-        const float4 m = mean[t];  // m.w: the forward's weight sum W
+    const bool act = valid && (gmx != 0.f || gmy != 0.f || gmz != 0.f);
+    if (__any_sync(0xffffffffu, act)) {
+        const float4 p = act ? sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
+        const float4 m = act ? mean[t] : make_float4(0.f, 0.f, 0.f, 1.f);  // m.w: the forward's weight sum W
         const Window w = narrow(window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
                                        cell1(p.z, sp.min[2], sp.cs), 2, sp),
                                 p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
         const float iw = 1.0f / m.w;
         const float gnx = gmx * iw, gny = gmy * iw, gnz = gmz * iw;
-        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-                const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
-                uint32_t beg = kEmpty, end = 0;
-                for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                    const uint2 r = __ldg(&ranges[c0 + xx]);
-                    if (r.x != kEmpty) {
-                        beg = min(beg, r.x);
-                        end = max(end, r.y);
-                    }
-                }
-                for (uint32_t i = beg; i < end; ++i) {
-                    const float4 q = __ldg(&sorted[i]);
-                    // the forward's neighbour decision, exactly
-                    const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
-                    if (!(d2 < R_lt2)) continue;
-                    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                    const float d = sqrtf(d2);
-                    const float s = d / R;
-                    const float wt = 1.0f - s * s * s;
-                    // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
-                    const float gw = gnx * (q.x - m.x) + gny * (q.y - m.y) + gnz * (q.z - m.z);
-                    float ex = 0.f, ey = 0.f, ez = 0.f;
-                    if (d > 0.f) {
-                        const float k = gw * (-3.0f * s * s / R) / d;  // dw/dd * (x_i - x_j)/d
-                        ex = k * dx;
-                        ey = k * dy;
-                        ez = k * dz;
-                    }
-                    gix += ex;
-                    giy += ey;
-                    giz += ez;
-                    atomicAdd(a.gx + i, make_float4(wt * gnx - ex, wt * gny - ey, wt * gnz - ez, 0.f));
-                }
+        walk_windows(w, act, coop_ok != 0, sp, ranges, sorted, s_q + (threadIdx.x & ~31u),
+                     [&](uint32_t i, const float4& q) {
+            // the forward's neighbour decision, exactly
+            const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+            if (!(d2 < R_lt2)) return;
+            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const float d = sqrtf(d2);
+            const float s = d / R;
+            const float wt = 1.0f - s * s * s;
+            // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
+            const float gw = gnx * (q.x - m.x) + gny * (q.y - m.y) + gnz * (q.z - m.z);
+            float ex = 0.f, ey = 0.f, ez = 0.f;
+            if (d > 0.f) {
+                const float k = gw * (-3.0f * s * s / R) / d;  // dw/dd * (x_i - x_j)/d
+                ex = k * dx;
+                ey = k * dy;
+                ez = k * dz;
             }
+            gix += ex;
+            giy += ey;
+            giz += ez;
+            atomicAdd(a.gx + i, make_float4(wt * gnx - ex, wt * gny - ey, wt * gnz - ez, 0.f));
+        });
     }
-    atomicAdd(a.gx + t, make_float4(gix, giy, giz, 0.f));
+    if (valid) atomicAdd(a.gx + t, make_float4(gix, giy, giz, 0.f));
 }
 
 __global__ void k_unsort(const float4* gx, const uint32_t* perm, uint32_t n, float* out)
@@ -605,8 +653,10 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
             k_field_backward_aniso<<<nblk(a.n), kT, 0, c.stream>>>(a);
         }
         k_cov_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, *cov);
+        // warps may walk the union of their windows when the cull radius stays below 2 cells
+        const int smooth_coop = (R * 1.0001f + 1e-4f * cov->sp.cs) < 2.0f * cov->sp.cs * 0.9999f ? 1 : 0;
         k_smooth_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, cov->sorted, cov->mean, cov->ranges, cov->sp, a.n, R,
-                                                           cov->R_lt2, lambda);
+                                                           cov->R_lt2, smooth_coop, lambda);
         g_launches += 3;
     } else if (method == FSR_METHOD_TC01) {
         k_field_backward_iso<true><<<nblk(a.n), kT, 0, c.stream>>>(a);

@@ -137,6 +137,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
         ca.min_neighbors = p.min_neighbors;
         ca.R_lt2 = sqrt_threshold(R, false);
         ca.R_le2 = sqrt_threshold(R, true);
+        // as in the forward: compact warps may walk the union of their windows
+        ca.coop_ok = (R + R * 1.0001f + 1e-4f * sp.cs) < 2.0f * sp.cs * 0.9999f ? 1 : 0;
     }
     const KernelCtx kc{st, h->num_sms};
     const bool want_radius = grad_particle_radius && (p.method == FSR_METHOD_ZB05 || p.method == FSR_METHOD_AKINCI12);
