@@ -133,9 +133,9 @@ __device__ uint32_t group_candidates(const Grid& sp, const uint2* __restrict__ r
 }
 
 // Candidate j of the group: its sorted particle index and window cell.
-__device__ __forceinline__ uint32_t candidate(uint32_t j, const CandTables& t, int* cell)
+__device__ __forceinline__ uint32_t candidate(uint32_t j, const CandTables& t, int* cell, int ncells = kMaxCells)
 {
-    int lo = 0, hi = kMaxCells;  // find k with cpre[k] <= j < cpre[k+1]
+    int lo = 0, hi = ncells;  // find k with cpre[k] <= j < cpre[k+1]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (t.cpre[mid] <= j) lo = mid;
@@ -180,9 +180,13 @@ struct WarpSlice {
     uint32_t cstart[128];
     uint32_t cpre[kMaxCells + 1];
     uint32_t cinv[128];
+    uint32_t ncells;             // entries of the candidate tables
+    uint32_t total_inv;          // candidates of involved cells (they come first)
 };
 
-// Warp-level version of group_candidates: the same cells, the same order.
+// Warp-level version of group_candidates: the same cells, listed with the
+// involved cells first and the other non-empty cells after them (each part
+// in window order); only non-empty kept cells get an entry.
 __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ranges,
                                     const uint8_t* __restrict__ invol, const float* __restrict__ reach,
                                     const int c[3], const float b0[3], const float b1[3], WarpSlice& w)
@@ -191,16 +195,17 @@ __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ra
     const int lx = clampi(c[0] - 2, 0, (int)sp.res[0] - 1), hx = clampi(c[0] + 2, 0, (int)sp.res[0] - 1);
     const int ly = clampi(c[1] - 2, 0, (int)sp.res[1] - 1), hy = clampi(c[1] + 2, 0, (int)sp.res[1] - 1);
     const int lz = clampi(c[2] - 2, 0, (int)sp.res[2] - 1), hz = clampi(c[2] + 2, 0, (int)sp.res[2] - 1);
-    uint32_t running = 0;
-    for (int k0 = 0; k0 < kMaxCells; k0 += 32) {
-        const int k = k0 + lane;
+    uint32_t st4[4], cnt4[4], inv4[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int k = 32 * r + lane;
         uint32_t cnt = 0, st = 0, inv = 0;
         if (k < kMaxCells) {
             const int xx = lx + k % 5, yy = ly + (k / 5) % 5, zz = lz + k / 25;
             if (xx <= hx && yy <= hy && zz <= hz) {
                 const uint32_t cell = lin3(xx, yy, zz, sp);
-                const uint2 r = __ldg(&ranges[cell]);
-                if (r.x != kEmpty) {
+                const uint2 rg = __ldg(&ranges[cell]);
+                if (rg.x != kEmpty) {
                     inv = __ldg(&invol[cell]);
                     bool keep = true;
                     if (inv) {
@@ -213,26 +218,47 @@ __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ra
                         keep = fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < cr * cr;
                     }
                     if (keep) {
-                        st = r.x;
-                        cnt = r.y - r.x;
+                        st = rg.x;
+                        cnt = rg.y - rg.x;
                     }
                 }
             }
         }
-        uint32_t x = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (k < kMaxCells) {
-            w.cstart[k] = st;
-            w.cinv[k] = inv;
-            w.cpre[k] = running + x - cnt;
-        }
-        running += __shfl_sync(0xffffffffu, x, 31);
+        st4[r] = st;
+        cnt4[r] = cnt;
+        inv4[r] = inv;
     }
-    if (lane == 0) w.cpre[kMaxCells] = running;
+    // two sweeps: involved cells, then the others; entries and prefix sums
+    // are appended in window order within each sweep
+    uint32_t running = 0, slot = 0;
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const bool take = cnt4[r] > 0 && (inv4[r] != 0) == (part == 0);
+            const uint32_t m = __ballot_sync(0xffffffffu, take);
+            const uint32_t c = take ? cnt4[r] : 0u;
+            uint32_t x = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (take) {
+                const uint32_t e = slot + __popc(m & ((1u << lane) - 1u));
+                w.cstart[e] = st4[r];
+                w.cinv[e] = inv4[r];
+                w.cpre[e] = running + x - c;
+            }
+            slot += __popc(m);
+            running += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (part == 0 && lane == 0) w.total_inv = running;
+    }
+    if (lane == 0) {
+        w.cpre[slot] = running;
+        w.ncells = slot;
+    }
     __syncwarp();
     return running;
 }
@@ -321,40 +347,34 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 ph.z = fmaxf(ph.z, __shfl_xor_sync(0xffffffffu, ph.z, o));
             }
             __syncwarp();
-            float sum[kPassTiles];
+            // two sums per vertex: the involved particles' terms, then the
+            // non-involved particles' (the unscaled kernel: about 1e-7 each,
+            // thousands of them), added among themselves and joined at the
+            // end, so that FP32 rounding does not drop or inflate them against
+            // a sum of order 1
+            float sum[kPassTiles], sum_u[kPassTiles];
 #pragma unroll
-            for (int t = 0; t < kPassTiles; ++t) sum[t] = 0.f;
-            for (uint32_t cb = 0; cb < total; cb += 32) {
+            for (int t = 0; t < kPassTiles; ++t) sum[t] = sum_u[t] = 0.f;
+            const uint32_t ncells = w.ncells, total_inv = w.total_inv;
+            // involved candidates: staged with their G, culled per tile by
+            // their support sphere, evaluated two at a time
+            for (uint32_t cb = 0; cb < total_inv; cb += 32) {
                 const uint32_t j = cb + lane;
                 bool keep = false;
                 float4 r0 = make_float4(0.f, 0.f, 0.f, -1.f);
-                if (j < total) {
+                if (j < total_inv) {
                     int cell;
-                    const uint32_t i = candidate(j, tabs, &cell);
-                    const bool inv = w.cinv[cell] != 0;
-                    if (inv) {
-                        r0 = __ldg(a.grec + 4ull * i);
-                    } else {
-                        const float4 s = __ldg(&a.smoothed[i]);
-                        r0 = make_float4(s.x, s.y, s.z, 1.0f);
-                    }
+                    const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
+                    const float4* gsrc = a.grec + 4ull * i;
+                    r0 = __ldg(gsrc);
                     keep = reaches(r0, pl, ph);
                     if (keep) {
                         float4* dst = w.rec + 4 * lane;
-                        if (inv) {
-                            const float4* gsrc = a.grec + 4ull * i;
-                            dst[1] = __ldg(gsrc + 1);
-                            dst[2] = __ldg(gsrc + 2);
-                            dst[3] = __ldg(gsrc + 3);
-                        } else {
-                            dst[1] = make_float4(1.f, 0.f, 0.f, a.sigma * __ldg(&a.smoothed[i].w));
-                            dst[2] = make_float4(0.f, 1.f, 0.f, 0.f);
-                            dst[3] = make_float4(0.f, 0.f, 1.f, 0.f);
-                        }
-                    } else {
-                        r0.w = -1.f;  // reaches no tile
+                        dst[0] = r0;
+                        dst[1] = __ldg(gsrc + 1);
+                        dst[2] = __ldg(gsrc + 2);
+                        dst[3] = __ldg(gsrc + 3);
                     }
-                    w.rec[4 * lane] = r0;
                 }
                 const uint32_t any = __ballot_sync(0xffffffffu, keep);
                 __syncwarp();
@@ -388,12 +408,55 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 }
                 __syncwarp();
             }
+            // non-involved candidates: G = I and support 1 (world units), which
+            // reaches every vertex of the window, so no culling; only the
+            // position and the coefficient sigma m / rho are staged, and q2 is
+            // |x~ - v|^2 (what the general path gives for G = I, bit for bit)
+            for (uint32_t cb = total_inv; cb < total; cb += 32) {
+                const uint32_t j = cb + lane;
+                if (j < total) {
+                    int cell;
+                    const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
+                    const float4 sm = __ldg(&a.smoothed[i]);
+                    w.rec[4 * lane] = make_float4(sm.x, sm.y, sm.z, a.sigma * sm.w);
+                }
+                const uint32_t cnt = min(32u, total - cb);
+                __syncwarp();
+#pragma unroll
+                for (int t = 0; t < kPassTiles; ++t) {
+                    const uint32_t v = 32 * t + lane;
+                    if ((uint32_t)t < ntiles && v < nv) {
+                        const float4 vp = w.vpos[v];
+                        float su = sum_u[t];
+                        uint32_t k = 0;
+                        for (; k + 2 <= cnt; k += 2) {
+                            const float4 qa = w.rec[4 * k], qb = w.rec[4 * (k + 1)];
+                            const float ax = qa.x - vp.x, ay = qa.y - vp.y, az = qa.z - vp.z;
+                            const float bx = qb.x - vp.x, by = qb.y - vp.y, bz = qb.z - vp.z;
+                            const float q2a = fmaf(ax, ax, fmaf(ay, ay, az * az));
+                            const float q2b = fmaf(bx, bx, fmaf(by, by, bz * bz));
+                            const float ua = 1.0f - q2a, ub = 1.0f - q2b;
+                            if (q2a < 1.0f) su = fmaf(qa.w, ua * ua * ua, su);
+                            if (q2b < 1.0f) su = fmaf(qb.w, ub * ub * ub, su);
+                        }
+                        if (k < cnt) {
+                            const float4 qa = w.rec[4 * k];
+                            const float ax = qa.x - vp.x, ay = qa.y - vp.y, az = qa.z - vp.z;
+                            const float q2a = fmaf(ax, ax, fmaf(ay, ay, az * az));
+                            const float ua = 1.0f - q2a;
+                            if (q2a < 1.0f) su = fmaf(qa.w, ua * ua * ua, su);
+                        }
+                        sum_u[t] = su;
+                    }
+                }
+                __syncwarp();
+            }
 #pragma unroll
             for (int t = 0; t < kPassTiles; ++t) {
                 const uint32_t v = 32 * t + lane;
                 if (v < nv) {
                     const uint32_t rank = __float_as_uint(w.vpos[v].w);
-                    if (rank < nb) a.phi[rank] = sum[t] - 0.5f;
+                    if (rank < nb) a.phi[rank] = (sum[t] + sum_u[t]) - 0.5f;
                 }
             }
             __syncwarp();

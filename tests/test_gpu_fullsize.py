@@ -1,0 +1,126 @@
+"""Checks on the 1M-particle anisotropic frame (the benchmark's workload) at full size.
+
+The oracle needs the dense scalar grid and takes minutes at this size, so the
+full-size frame is checked through properties that hold at any size:
+
+* the field at 1,000 sampled band vertices equals an FP64 evaluation of the
+  anisotropic kernel sum (computationOfScalarFieldGrid, ReconstructionCUDA.cu:
+  830-906) over the same +-2-cell window, given the frame's own smoothed
+  positions and G matrices (those two stages are checked against the oracle
+  in test_gpu_parity.py), within 1e-5 relative to max(1, |phi|);
+* a frame run twice gives the same mesh, bit for bit;
+* every mesh vertex lies on a scalar-grid edge (two of its coordinates are grid
+  coordinates, computed as getVertexPos does in FP32), and normals are unit
+  vectors (all but the few next to the fill value, where the reference's FP32
+  gradient overflows).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = dict(smoothing_lambda=0.9, aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0)
+SIGMA = np.float32(315.0) / (np.float32(64.0) * np.float32(3.1415926535898))
+
+
+@pytest.fixture(scope="module")
+def frame():
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api, synthetic
+    fr = synthetic.dam_break(1 << 20, r=0.004, seed=2)
+    rec = api.Reconstructor("yu13", 0, keep_intermediates=True, **SETTINGS)
+    x = torch.from_numpy(fr.pos).cuda()
+    d = torch.from_numpy(fr.density).cuda()
+    rec.reconstruct(x, d, api.header_of(fr))
+    out = dict(fr=fr, stats=rec.stats(), mesh=rec.mesh(), band=rec.debug("band"), field=rec.debug("field"),
+               sorted=rec.debug("sorted_xyz"), ranges=rec.debug("ranges"), inv=rec.debug("involved_counts"),
+               smoothed=rec.debug("smoothed"), G=rec.debug("G"))
+    rec.reconstruct(x, d, api.header_of(fr))
+    out["mesh2"] = rec.mesh()
+    rec.close()
+    return out
+
+
+def _grids(fr):
+    from oracle import pipeline as P
+    sp, sc = P.grid_derive(fr.bbox_min, fr.bbox_max, fr.h, SETTINGS["cell_size_scale"], SETTINGS["grid_ratio"])
+    return sp, sc
+
+
+def test_field_matches_fp64_kernel_sum(frame):
+    fr = frame["fr"]
+    sp, sc = _grids(fr)
+    spmin = np.array(sp.minPos, np.float32)
+    scmin = np.array(sc.minPos, np.float32)
+    spcs, sccs = np.float32(sp.cellSize), np.float32(sc.cellSize)
+    sres = np.array(sp.res, np.int64)
+    vres = np.array(sc.res, np.int64)
+    assert list(frame["stats"].spatial_res) == list(sres) and list(frame["stats"].scalar_res) == list(vres)
+    ranges, inv = frame["ranges"], frame["inv"]
+    sm = frame["smoothed"].astype(np.float64)
+    G = frame["G"].reshape(-1, 3, 3).astype(np.float64)
+    m_rho = np.float32(fr.mass) / fr.density.astype(np.float32)  # __fdiv_rn(mass, rho)
+    assert np.all(fr.density == fr.density[0])
+    coef_plain = float(SIGMA * m_rho[0])
+    rng = np.random.default_rng(7)
+    pick = rng.choice(frame["band"].size, 1000, replace=False)
+    worst = 0.0
+    for r in pick:
+        v = int(frame["band"][r])
+        idx = np.array([v % vres[0], (v // vres[0]) % vres[1], v // (vres[0] * vres[1])])
+        vp = (idx.astype(np.float32) * sccs).astype(np.float32) + scmin           # getVertexPos in FP32
+        c = np.trunc(((vp - spmin).astype(np.float32) / spcs).astype(np.float32)).astype(np.int64)
+        lo, hi = np.clip(c - 2, 0, sres - 1), np.clip(c + 2, 0, sres - 1)
+        parts, flags = [], []
+        for z in range(lo[2], hi[2] + 1):
+            for y in range(lo[1], hi[1] + 1):
+                for x in range(lo[0], hi[0] + 1):
+                    cell = x + sres[0] * (y + sres[1] * z)
+                    a, b = ranges[cell]
+                    if a == 0xFFFFFFFF:
+                        continue
+                    parts.append(np.arange(a, b))
+                    flags.append(np.full(b - a, inv[cell] > 0))
+        if not parts:
+            phi64 = -0.5
+        else:
+            j = np.concatenate(parts)
+            involved = np.concatenate(flags)
+            rv = sm[j] - vp.astype(np.float64)
+            t = np.where(involved[:, None], np.einsum("nij,nj->ni", G[j], rv), rv)
+            q2 = np.sum(t * t, axis=1)
+            det = np.linalg.det(G[j])
+            coef = np.where(involved, float(SIGMA) * det * float(m_rho[0]), coef_plain)
+            u = 1.0 - q2
+            phi64 = float(np.sum(np.where(q2 < 1.0, coef * u * u * u, 0.0))) - 0.5
+        err = abs(float(frame["field"][r]) - phi64) / max(1.0, abs(phi64))
+        worst = max(worst, err)
+    assert worst <= 1e-5, worst
+
+
+def test_frame_is_deterministic(frame):
+    a, b = frame["mesh"], frame["mesh2"]
+    assert a.positions.shape == b.positions.shape
+    assert np.array_equal(a.positions, b.positions) and np.array_equal(a.normals, b.normals)
+
+
+def test_mesh_vertices_on_grid_edges(frame):
+    fr = frame["fr"]
+    _, sc = _grids(fr)
+    scmin = np.array(sc.minPos, np.float32)
+    sccs = np.float32(sc.cellSize)
+    pos, nrm = frame["mesh"].positions, frame["mesh"].normals
+    assert pos.shape[0] == frame["stats"].n_mesh_vertices and pos.shape[0] % 3 == 0
+    on_grid = np.zeros(pos.shape, bool)
+    for a in range(3):
+        i = np.rint((pos[:, a] - scmin[a]) / sccs).astype(np.int64)
+        for di in (-1, 0, 1):
+            g = ((i + di).astype(np.float32) * sccs).astype(np.float32) + scmin[a]
+            on_grid[:, a] |= g == pos[:, a]
+    assert np.all(on_grid.sum(axis=1) >= 2)
+    # normals are normalised field gradients; next to the anisotropic path's
+    # fill value (1.7e22 off the band) the reference's FP32 gradient can
+    # overflow, which leaves a few normals that are not unit vectors
+    ln = np.linalg.norm(nrm.astype(np.float64), axis=1)
+    unit = np.abs(ln - 1.0) < 1e-5
+    assert unit.mean() >= 0.999, unit.mean()
