@@ -650,6 +650,24 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
             const float coef = g0.w;
             float gxs = 0.f, gys = 0.f, gzs = 0.f, sc = 0.f;
             float gg[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (!inv) {
+                // unscaled kernel (G = I, support 1): d/dx~ (1 - |r|^2)^3 = -6 (1 - |r|^2)^2 r;
+                // no dL/dG.  Candidates come cell by cell, so a warp's threads
+                // mostly take the same branch.
+                for (uint32_t q = 0; q < nv; ++q) {
+                    const float4 v = av[q];
+                    const float rx = r0.x - v.x, ry = r0.y - v.y, rz = r0.z - v.z;
+                    const float q2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
+                    if (!(q2 < 1.0f)) continue;
+                    const float u = 1.0f - q2;
+                    const float A = -6.0f * v.w * coef * u * u;
+                    gxs = fmaf(A, rx, gxs);
+                    gys = fmaf(A, ry, gys);
+                    gzs = fmaf(A, rz, gzs);
+                }
+                if (gxs != 0.f || gys != 0.f || gzs != 0.f) atomicAdd(a.gsmooth + i, make_float4(gxs, gys, gzs, 0.f));
+                continue;
+            }
             for (uint32_t k = 0; k < nch; ++k) {
                 if (!(box_dist2(r0.x, r0.y, r0.z, cbox[2 * k], cbox[2 * k + 1]) < r0.w)) continue;
                 const uint32_t qe = min(nv, 32 * k + 32);
