@@ -277,6 +277,117 @@ def run_reference(args, w, fr):
     print(json.dumps(line), flush=True)
 
 
+def _write_xyz_text(path, fr):
+    """.xyz text of a frame (%.9g, data_format.txt layout), written with numpy."""
+    with open(path, "w") as f:
+        f.write("%.9g %.9g %.9g\n" % tuple(fr.bbox_min))
+        f.write("%.9g %.9g %.9g\n" % tuple(fr.bbox_max))
+        f.write("%.9g\n%.9g\n%.9g\n" % (fr.h, fr.particle_radius, fr.mass))
+        np.savetxt(f, np.concatenate([fr.pos, fr.density[:, None]], axis=1).astype(np.float64), fmt="%.9g")
+
+
+def _best_ms(fn, reps):
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        best = min(best, (time.perf_counter() - t0) * 1e3)
+    return best
+
+
+def run_io_leg(args, w):
+    """File-driven frames (.xyz in, .obj out) through the reference's
+    interface, with the library's parallel reader and writer, the .xyzb
+    sidecar and the read/compute/write overlap; beside them the reference's
+    stream-based reader and writer (oracle/io_port.cpp, one thread)."""
+    import ctypes
+    import shutil
+    import tempfile
+    from fluidsurfacereconstructiongpu_gb300 import api
+    fr = make_frame(w)
+    d = tempfile.mkdtemp(prefix="fsr_io_")
+    nfr = 3
+    try:
+        for k in range(nfr):
+            _write_xyz_text(os.path.join(d, "frame_%03d.xyz" % k), fr)
+        x0 = os.path.join(d, "frame_000.xyz")
+        cores = os.cpu_count() or 1
+        io = {"particles": int(fr.n), "xyz_bytes": os.path.getsize(x0), "threads": cores}
+        api.set_io_threads(1)
+        io["read_xyz_ms_1thread"] = _best_ms(lambda: api.read_xyz(x0), 2)
+        api.set_io_threads(0)
+        io["read_xyz_ms"] = _best_ms(lambda: api.read_xyz(x0), 3)
+        hdr, xyz, den = api.read_xyz(x0)
+        b0 = os.path.join(d, "frame_000.xyzb")
+        api.write_xyz_binary(b0, hdr, xyz, den)
+        io["read_xyzb_ms"] = _best_ms(lambda: api.read_xyz_binary(b0), 3)
+        port = ctypes.CDLL(os.path.join(ROOT, "oracle", "_build", "libio_port.so"))
+        port.io_port_read_xyz.restype = ctypes.c_int64
+        port.io_port_read_xyz.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+        port.io_port_write_obj.restype = ctypes.c_int
+        port.io_port_write_obj.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+        hbuf = np.zeros(9, np.float32)
+        pbuf = np.zeros((fr.n, 4), np.float32)
+        io["port_read_xyz_ms"] = _best_ms(
+            lambda: port.io_port_read_xyz(x0.encode(), hbuf.ctypes.data, pbuf.ctypes.data, fr.n), 1)
+        assert np.array_equal(pbuf[:, :3], xyz) and np.array_equal(pbuf[:, 3], den)
+        # one frame's mesh for the writers
+        import torch
+        rec = api.Reconstructor(w["method"], 0, **recon_kwargs(w))
+        rec.reconstruct(torch.from_numpy(xyz).cuda(), torch.from_numpy(den).cuda(), hdr)
+        mesh = rec.mesh()
+        rec.close()
+        o1 = os.path.join(d, "m.obj")
+        api.set_io_threads(1)
+        io["write_obj_ms_1thread"] = _best_ms(lambda: api.write_obj(o1, mesh), 1)
+        api.set_io_threads(0)
+        io["write_obj_ms"] = _best_ms(lambda: api.write_obj(o1, mesh), 3)
+        io["obj_bytes"] = os.path.getsize(o1)
+        o2 = os.path.join(d, "port.obj")
+        pos = np.ascontiguousarray(mesh.positions, np.float32)
+        nrm = np.ascontiguousarray(mesh.normals, np.float32)
+        io["port_write_obj_ms"] = _best_ms(
+            lambda: port.io_port_write_obj(o2.encode(), pos.ctypes.data, nrm.ctypes.data, pos.shape[0]), 1)
+        with open(o1, "rb") as f1, open(o2, "rb") as f2:
+            io["obj_identical_to_port"] = f1.read() == f2.read()
+        os.remove(b0)
+        # the file-driven loop: text, then with sidecars (made by a first run)
+        loop = api.ReconstructorGPUOursYu13(d + os.sep, "frame_%03d", 0, nfr, **recon_kwargs(w))
+        loop.setOutputMeshFile(True)
+        loop.reconstruct()  # warm-up
+        loop.reconstruct()
+        t_text = loop.ioTiming()
+        loop.setBinarySidecar(True)
+        loop.reconstruct()  # writes the sidecars
+        loop.reconstruct()
+        t_side = loop.ioTiming()
+        fields = ("read_ms", "upload_ms", "reconstruct_ms", "write_ms", "wall_ms")
+        io["loop_text"] = {k: getattr(t_text, k) / nfr for k in fields}
+        io["loop_sidecar"] = {k: getattr(t_side, k) / nfr for k in fields}
+        # the reference's loop, serial: stream reader + frame + stream writer
+        serial_ms = io["port_read_xyz_ms"] + io["loop_text"]["upload_ms"] + io["loop_text"]["reconstruct_ms"] + \
+            io["port_write_obj_ms"]
+        out = {
+            "metric": "frames/s file-driven (.xyz -> mesh -> .obj) @1M aniso",
+            "value": 1e3 / io["loop_sidecar"]["wall_ms"],
+            "unit": "frames/s",
+            "n_gpus": 1,
+            "frames": nfr,
+            "higher_is_better": True,
+            "data": "synthetic (%s N=%d, seeded; %%.9g text)" % (w["kind"], fr.n),
+            "config": {"workload": args.workload, "method": w["method"]},
+            "text_value": 1e3 / io["loop_text"]["wall_ms"],
+            "cpu_baseline": {"value": 1e3 / serial_ms, "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": "the reference's stream reader and writer (one thread) around this "
+                                       "library's frame, no overlap"},
+            "io": io,
+        }
+        print(json.dumps(out))
+    finally:
+        api.set_io_threads(0)
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,9 +400,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-backward", action="store_true", help="skip the forward+backward leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames leg")
+    ap.add_argument("--io", action="store_true",
+                    help="time the file-driven loop (.xyz in, .obj out) instead of the in-memory frame")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.io:
+        run_io_leg(args, w)
+        return
 
     if args.impl == "reference":
         fr = make_frame(w)

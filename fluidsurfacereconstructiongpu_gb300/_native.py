@@ -74,6 +74,14 @@ class BatchTuning(ctypes.Structure):
 BATCH_RETUNE = 0x1
 BATCH_NO_AUTOTUNE = 0x2
 
+FILES_WRITE_OBJ = 0x1
+FILES_SIDECAR = 0x2
+
+
+class FilesTiming(ctypes.Structure):
+    _fields_ = [("read_ms", ctypes.c_double), ("upload_ms", ctypes.c_double), ("reconstruct_ms", ctypes.c_double),
+                ("write_ms", ctypes.c_double), ("wall_ms", ctypes.c_double)]
+
 
 def _load():
     if not os.path.exists(LIB_PATH):
@@ -110,6 +118,11 @@ def _load():
         "fsr_write_obj": (ctypes.c_int, [ctypes.c_char_p, c_vp, c_vp, c_u64]),
         "fsr_reconstruct_files": (ctypes.c_int, [c_vp, ctypes.c_char_p, ctypes.c_char_p, c_u32, c_u32,
                                                  ctypes.c_int, P(ctypes.c_double)]),
+        "fsr_reconstruct_files_ex": (ctypes.c_int, [c_vp, ctypes.c_char_p, ctypes.c_char_p, c_u32, c_u32, c_u32,
+                                                    P(ctypes.c_double), P(FilesTiming)]),
+        "fsr_io_set_threads": (None, [c_u32]),
+        "fsr_write_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), c_vp, c_vp, c_u64]),
+        "fsr_read_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

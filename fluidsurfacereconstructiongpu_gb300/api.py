@@ -287,12 +287,35 @@ class Batch:
         return Mesh(pos[:nv], nrm[:nv])
 
 
+def set_io_threads(n: int) -> None:
+    """Host threads of the .xyz reader and .obj writer (0: one per core)."""
+    N.lib.fsr_io_set_threads(int(n))
+
+
 def read_xyz(path: str):
     """Parses an .xyz file; returns (header, xyz (N,3), density (N,))."""
+    return _read_particles(N.lib.fsr_read_xyz, path)
+
+
+def read_xyz_binary(path: str):
+    """Reads an .xyzb sidecar; returns (header, xyz (N,3), density (N,))."""
+    return _read_particles(N.lib.fsr_read_xyz_binary, path)
+
+
+def write_xyz_binary(path: str, header, xyz, density) -> None:
+    """Writes particles as an .xyzb file (the binary form of an .xyz)."""
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    den = np.ascontiguousarray(density, np.float32).reshape(-1)
+    if den.shape[0] != xyz.shape[0]:
+        raise ValueError("xyz and density differ in length")
+    N.check(N.lib.fsr_write_xyz_binary(path.encode(), ctypes.byref(header), xyz.ctypes.data, den.ctypes.data,
+                                       xyz.shape[0]))
+
+
+def _read_particles(fn, path: str):
     hd = N.FrameHeader()
     px, pd, n = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_uint64()
-    N.check(N.lib.fsr_read_xyz(path.encode(), ctypes.byref(hd), ctypes.byref(px), ctypes.byref(pd),
-                               ctypes.byref(n)))
+    N.check(fn(path.encode(), ctypes.byref(hd), ctypes.byref(px), ctypes.byref(pd), ctypes.byref(n)))
     try:
         cnt = n.value
         xyz = np.ctypeslib.as_array((ctypes.c_float * (3 * max(cnt, 1))).from_address(px.value))[:3 * cnt]
@@ -339,6 +362,8 @@ class ReconstructorGPU:
         self._rec = Reconstructor(self.METHOD, device, **params)
         self._times: list[float] = []
         self._num_particles = 0
+        self._sidecar = False
+        self._io = None
 
     def getAlgorithmType(self) -> str:
         return self.ALGORITHM
@@ -352,6 +377,15 @@ class ReconstructorGPU:
     def setOutputVisualizeFile(self, flag: bool):
         if flag:
             raise NotImplementedError(".vis debug dumps are not produced by this library")
+
+    def setBinarySidecar(self, flag: bool):
+        """Read stem.xyzb instead of parsing stem.xyz when it is current, and
+        write it after parsing (FSR_FILES_SIDECAR)."""
+        self._sidecar = bool(flag)
+
+    def ioTiming(self):
+        """Host timings of the last reconstruct() (fsr_files_timing)."""
+        return self._io
 
     def getSimulationParameters(self) -> N.Params:
         return self._rec.params
@@ -368,9 +402,12 @@ class ReconstructorGPU:
         n = self.frame_to - self.frame_from
         ms = (ctypes.c_double * n)()
         d = self.directory if self.directory.endswith(os.sep) or not self.directory else self.directory + os.sep
-        st = N.lib.fsr_reconstruct_files(self._rec._h, d.encode(), self.file_pattern.encode(),
-                                         self.frame_from, self.frame_to, 1 if self._save_obj else 0, ms)
+        flags = (N.FILES_WRITE_OBJ if self._save_obj else 0) | (N.FILES_SIDECAR if self._sidecar else 0)
+        tm = N.FilesTiming()
+        st = N.lib.fsr_reconstruct_files_ex(self._rec._h, d.encode(), self.file_pattern.encode(),
+                                            self.frame_from, self.frame_to, flags, ms, ctypes.byref(tm))
         N.check(st, self._rec._h)
+        self._io = tm
         self._times = list(ms)
         if self._save_cfg:
             s = self._rec.stats()

@@ -302,9 +302,26 @@ fsr_status fsr_read_xyz(const char* path, fsr_frame_header* hdr, float** xyz, fl
 void fsr_free_host(void* p);
 
 /* Writes a triangle soup as .obj: v lines, vn lines, then
- * "f i//i i+1//i+1 i+2//i+2" per triangle (ReconstructorGPUOurs.cpp:58-99). */
+ * "f i//i i+1//i+1 i+2//i+2" per triangle (ReconstructorGPUOurs.cpp:58-99),
+ * numbers as std::ostream prints them (%g, 6 significant digits).  Lines are
+ * formatted by all I/O threads; the bytes do not depend on their number. */
 fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm,
                          uint64_t n_vertices);
+
+/* Host threads of fsr_read_xyz and fsr_write_obj (0, the default: one per
+ * core, at most 64). */
+void fsr_io_set_threads(uint32_t n);
+
+/* .xyzb, the binary sidecar of an .xyz file: an 80-byte header (magic
+ * "FSRXYZB1", u64 particle count, u64 size and i64 modification time in ns of
+ * the .xyz it was made from, 9 header floats: bbox min, bbox max, h,
+ * particle radius, particle mass, 12 bytes of padding), then n x 3 float
+ * positions and n float densities, little-endian.  The same numbers as the
+ * .xyz, read without parsing text.  Buffers as for fsr_read_xyz. */
+fsr_status fsr_write_xyz_binary(const char* path, const fsr_frame_header* hdr, const float* xyz,
+                                const float* density, uint64_t n);
+fsr_status fsr_read_xyz_binary(const char* path, fsr_frame_header* hdr, float** xyz, float** density,
+                               uint64_t* n);
 
 /* File-driven frame loop of ReconstructorGPU::reconstruct (ReconstructorGPU.cpp:
  * 25-79): frames [from, to) of directory + printf(pattern, frame) + ".xyz",
@@ -313,6 +330,30 @@ fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm,
  * frame_ms[0 .. to-from) when frame_ms is not NULL. */
 fsr_status fsr_reconstruct_files(fsr_handle* h, const char* directory, const char* pattern,
                                  uint32_t from, uint32_t to, int write_obj, double* frame_ms);
+
+/* Flags of fsr_reconstruct_files_ex. */
+#define FSR_FILES_WRITE_OBJ 0x1u /* write stem.obj per frame */
+/* Read stem.xyzb instead of parsing stem.xyz when the sidecar was made from
+ * the .xyz as it is now (same size and modification time); after parsing an
+ * .xyz, write its sidecar (best effort). */
+#define FSR_FILES_SIDECAR 0x2u
+
+/* Host milliseconds of a file-driven run, summed over its frames.  Reading
+ * and writing overlap the GPU work (frame k + 1 is read and frame k - 1's
+ * .obj written while frame k runs), so wall_ms is less than the sum. */
+typedef struct fsr_files_timing {
+    double read_ms;        /* .xyz parse or .xyzb read */
+    double upload_ms;      /* host -> device copies */
+    double reconstruct_ms; /* the reference's timer scope, hashing to mesh */
+    double write_ms;       /* .obj formatting and writing */
+    double wall_ms;        /* the whole call */
+} fsr_files_timing;
+
+/* fsr_reconstruct_files with FSR_FILES_* flags and host timings (timing may be
+ * NULL). */
+fsr_status fsr_reconstruct_files_ex(fsr_handle* h, const char* directory, const char* pattern,
+                                    uint32_t from, uint32_t to, uint32_t flags, double* frame_ms,
+                                    fsr_files_timing* timing);
 
 #ifdef __cplusplus
 }

@@ -71,8 +71,9 @@ public:
         std::vector<double> tri, spr, svr, es, sf, mc;
         for (unsigned int f = mFrom; f < mTo; ++f) {
             double ms = 0.0;
-            check(fsr_reconstruct_files(mHandle, mDirectory.c_str(), mPattern.c_str(), f, f + 1,
-                                        mSaveObjFile ? 1 : 0, &ms),
+            const uint32_t flags = (mSaveObjFile ? FSR_FILES_WRITE_OBJ : 0u) | (mSidecar ? FSR_FILES_SIDECAR : 0u);
+            check(fsr_reconstruct_files_ex(mHandle, mDirectory.c_str(), mPattern.c_str(), f, f + 1, flags, &ms,
+                                           nullptr),
                   "frame " + std::to_string(f));
             mTimeConsuming.push_back(ms);
             fsr_stats st;
@@ -96,6 +97,9 @@ public:
     void setOutputMeshFile(bool flag) { mSaveObjFile = flag; }
     void setOutputConfigFile(bool flag) { mSaveCfgFile = flag; }
     void setOutputVisualizeFile(bool flag) { mSaveVisFile = flag; }
+    /* Read stem.xyzb instead of parsing stem.xyz when it is current, and
+     * write it after parsing (FSR_FILES_SIDECAR). */
+    void setBinarySidecar(bool flag) { mSidecar = flag; }
 
     SimParam getSimulationParameters() const
     {
@@ -165,7 +169,7 @@ protected:
     std::string mDirectory, mPattern;
     unsigned int mFrom, mTo;
     int mDevice;
-    bool mSaveObjFile = true, mSaveVisFile = false, mSaveCfgFile = false;
+    bool mSaveObjFile = true, mSaveVisFile = false, mSaveCfgFile = false, mSidecar = false;
     fsr_params mParams{};
     fsr_handle* mHandle = nullptr;
     fsr_frame_header mHeader{};

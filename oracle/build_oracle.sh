@@ -1,6 +1,8 @@
 #!/usr/bin/env bash
 # Builds the CPU oracle (test infrastructure): oracle/_build/liboracle32.so
-# (reference FP32 semantics) and liboracle64.so (FP64 continuous values).
+# (reference FP32 semantics), liboracle64.so (FP64 continuous values) and
+# libio_port.so (the reference's stream-based .xyz reader and .obj writer,
+# the file formats' timing baseline).
 # -ffp-contract=off keeps every multiply and add separately rounded, as the
 # reference source is written (aarch64 gcc would otherwise fuse them).
 set -euo pipefail
@@ -13,6 +15,9 @@ FLAGS=(-std=c11 -O2 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -Wal
 P1=$!
 "$CC" "${FLAGS[@]}" -DFSR_REAL_BITS=64 -o "$OUT/liboracle64.so" "$HERE/fsr_oracle.c" -lm &
 P2=$!
+"${CXX:-g++}" -std=c++17 -O2 -fPIC -shared -o "$OUT/libio_port.so" "$HERE/io_port.cpp" &
+P3=$!
 wait "$P1"
 wait "$P2"
-echo "build_oracle: wrote $OUT/liboracle32.so $OUT/liboracle64.so"
+wait "$P3"
+echo "build_oracle: wrote $OUT/liboracle32.so $OUT/liboracle64.so $OUT/libio_port.so"
