@@ -361,9 +361,15 @@ def run_io_leg(args, w):
         loop.reconstruct()  # writes the sidecars
         loop.reconstruct()
         t_side = loop.ioTiming()
+        loop.setIndexedMesh(True)  # welded meshes (FSR_FLAG_WELD), indexed .obj
+        loop.reconstruct()
+        loop.reconstruct()
+        t_weld = loop.ioTiming()
+        io["indexed_obj_bytes"] = os.path.getsize(os.path.join(d, "frame_000.obj"))
         fields = ("read_ms", "upload_ms", "reconstruct_ms", "write_ms", "wall_ms")
         io["loop_text"] = {k: getattr(t_text, k) / nfr for k in fields}
         io["loop_sidecar"] = {k: getattr(t_side, k) / nfr for k in fields}
+        io["loop_sidecar_indexed"] = {k: getattr(t_weld, k) / nfr for k in fields}
         # the reference's loop, serial: stream reader + frame + stream writer
         serial_ms = io["port_read_xyz_ms"] + io["loop_text"]["upload_ms"] + io["loop_text"]["reconstruct_ms"] + \
             io["port_write_obj_ms"]
@@ -377,6 +383,7 @@ def run_io_leg(args, w):
             "data": "synthetic (%s N=%d, seeded; %%.9g text)" % (w["kind"], fr.n),
             "config": {"workload": args.workload, "method": w["method"]},
             "text_value": 1e3 / io["loop_text"]["wall_ms"],
+            "indexed_value": 1e3 / io["loop_sidecar_indexed"]["wall_ms"],
             "cpu_baseline": {"value": 1e3 / serial_ms, "unit": "frames/s", "cores": 1, "kind": "port",
                              "sample": "the reference's stream reader and writer (one thread) around this "
                                        "library's frame, no overlap"},

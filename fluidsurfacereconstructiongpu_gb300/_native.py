@@ -26,9 +26,10 @@ METHOD_ZB05, METHOD_TC01, METHOD_YU13, METHOD_AKINCI12 = 0, 1, 2, 3
 FLAG_KEEP_INTERMEDIATES = 0x1
 FLAG_STAGE_TIMING = 0x2
 FLAG_SMALL_POOLS = 0x4
+FLAG_WELD = 0x8
 
 DBG = dict(perm=0, sorted_xyz=1, ranges=2, surface_flags=3, involved_counts=4, band=5, field=6,
-           mc_info=7, valid=8, mean=9, smoothed=10, G=11)
+           mc_info=7, valid=8, mean=9, smoothed=10, G=11, weld_keys=12)
 
 NUM_STAGES = 12
 STAGE_NAMES = ["hash+sort", "ranges", "surface", "band stamp", "band list", "smoothing", "covariance",
@@ -52,7 +53,8 @@ class Stats(ctypes.Structure):
                 ("n_valid_cubes", c_u64), ("n_mesh_vertices", c_u64), ("spatial_res", c_u32 * 3),
                 ("scalar_res", c_u32 * 3), ("n_fp64_fallbacks", c_u32), ("n_retries", c_u32),
                 ("n_kernel_launches", c_u32), ("n_backward_launches", c_u32),
-                ("stage_ms", c_f32 * NUM_STAGES), ("total_ms", c_f32), ("device_bytes", c_u64)]
+                ("stage_ms", c_f32 * NUM_STAGES), ("total_ms", c_f32), ("device_bytes", c_u64),
+                ("n_weld_vertices", c_u64)]
 
 
 class FsrError(RuntimeError):
@@ -76,6 +78,7 @@ BATCH_NO_AUTOTUNE = 0x2
 
 FILES_WRITE_OBJ = 0x1
 FILES_SIDECAR = 0x2
+FILES_INDEXED_OBJ = 0x4
 
 
 class FilesTiming(ctypes.Structure):
@@ -121,6 +124,8 @@ def _load():
         "fsr_reconstruct_files_ex": (ctypes.c_int, [c_vp, ctypes.c_char_p, ctypes.c_char_p, c_u32, c_u32, c_u32,
                                                     P(ctypes.c_double), P(FilesTiming)]),
         "fsr_io_set_threads": (None, [c_u32]),
+        "fsr_copy_indexed_mesh": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, c_vp, c_u64, P(c_u64), P(c_u64)]),
+        "fsr_write_obj_indexed": (ctypes.c_int, [ctypes.c_char_p, c_vp, c_vp, c_u64, c_vp, c_u64]),
         "fsr_write_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), c_vp, c_vp, c_u64]),
         "fsr_read_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
     }

@@ -57,6 +57,13 @@ class Mesh:
         return self.positions.shape[0] // 3
 
 
+@dataclass
+class IndexedMesh:
+    positions: np.ndarray  # (V, 3) f32, shared vertices in order of first use
+    normals: np.ndarray
+    triangles: np.ndarray  # (T, 3) u32 vertex indices, the soup's triangle order
+
+
 class Reconstructor:
     """One reconstructor handle bound to a CUDA device."""
 
@@ -64,7 +71,7 @@ class Reconstructor:
                  grid_ratio: Optional[int] = None, cell_size_scale: Optional[float] = None,
                  smoothing_lambda: Optional[float] = None, aniso_radius_over_h: Optional[float] = None,
                  min_neighbors: Optional[int] = None, keep_intermediates: bool = False,
-                 stage_timing: bool = False):
+                 stage_timing: bool = False, weld: bool = False):
         self.method = method
         p = default_params(method)
         if iso is not None:
@@ -80,7 +87,7 @@ class Reconstructor:
         if min_neighbors is not None:
             p.min_neighbors = min_neighbors
         p.flags = (N.FLAG_KEEP_INTERMEDIATES if keep_intermediates else 0) | \
-            (N.FLAG_STAGE_TIMING if stage_timing else 0)
+            (N.FLAG_STAGE_TIMING if stage_timing else 0) | (N.FLAG_WELD if weld else 0)
         self.params = p
         h = ctypes.c_void_p()
         st = N.lib.fsr_create(ctypes.byref(p), int(device), ctypes.byref(h))
@@ -189,10 +196,27 @@ class Reconstructor:
         N.check(N.lib.fsr_get_stats(self._h, ctypes.byref(s)), self._h)
         return s
 
+    def indexed_mesh(self) -> "IndexedMesh":
+        """The last frame's welded mesh (needs weld=True)."""
+        s = self.stats()
+        nv, ni = int(s.n_weld_vertices), int(s.n_mesh_vertices)
+        pos = np.empty((nv, 3), np.float32)
+        nrm = np.empty((nv, 3), np.float32)
+        idx = np.empty(ni, np.uint32)
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        N.check(N.lib.fsr_copy_indexed_mesh(self._h, pos.ctypes.data, nrm.ctypes.data, nv, idx.ctypes.data, ni,
+                                            ctypes.byref(a), ctypes.byref(b)), self._h)
+        return IndexedMesh(pos, nrm, idx.reshape(-1, 3))
+
     def debug(self, name: str) -> np.ndarray:
         which = N.DBG[name]
         need = ctypes.c_uint64(0)
         N.check(N.lib.fsr_debug_fetch(self._h, which, None, 0, ctypes.byref(need)), self._h)
+        if name == "weld_keys":
+            out = np.empty(need.value // 8, dtype=np.uint64)
+            if need.value:
+                N.check(N.lib.fsr_debug_fetch(self._h, which, out.ctypes.data, need.value, None), self._h)
+            return out
         dtype = np.float32 if name in ("sorted_xyz", "field", "mean", "smoothed", "G") else np.uint32
         out = np.empty(need.value // 4, dtype=dtype)
         if need.value:
@@ -338,9 +362,15 @@ def write_xyz(path: str, frame) -> None:
             f.write("%.9g %.9g %.9g %.9g\n" % (p[0], p[1], p[2], d))
 
 
-def write_obj(path: str, mesh: Mesh) -> None:
+def write_obj(path: str, mesh) -> None:
+    """Writes a Mesh (triangle soup) or an IndexedMesh as .obj."""
     pos = np.ascontiguousarray(mesh.positions, np.float32)
     nrm = np.ascontiguousarray(mesh.normals, np.float32)
+    if isinstance(mesh, IndexedMesh):
+        idx = np.ascontiguousarray(mesh.triangles, np.uint32).reshape(-1)
+        N.check(N.lib.fsr_write_obj_indexed(path.encode(), pos.ctypes.data, nrm.ctypes.data, pos.shape[0],
+                                            idx.ctypes.data, idx.shape[0]))
+        return
     N.check(N.lib.fsr_write_obj(path.encode(), pos.ctypes.data, nrm.ctypes.data, pos.shape[0]))
 
 
@@ -363,6 +393,7 @@ class ReconstructorGPU:
         self._times: list[float] = []
         self._num_particles = 0
         self._sidecar = False
+        self._indexed = False
         self._io = None
 
     def getAlgorithmType(self) -> str:
@@ -377,6 +408,13 @@ class ReconstructorGPU:
     def setOutputVisualizeFile(self, flag: bool):
         if flag:
             raise NotImplementedError(".vis debug dumps are not produced by this library")
+
+    def setIndexedMesh(self, flag: bool):
+        """Write welded (indexed) .obj files instead of triangle soups."""
+        self._indexed = bool(flag)
+        p = self._rec.params
+        p.flags = (p.flags | N.FLAG_WELD) if flag else (p.flags & ~N.FLAG_WELD)
+        N.check(N.lib.fsr_set_params(self._rec._h, ctypes.byref(p)), self._rec._h)
 
     def setBinarySidecar(self, flag: bool):
         """Read stem.xyzb instead of parsing stem.xyz when it is current, and
@@ -402,7 +440,8 @@ class ReconstructorGPU:
         n = self.frame_to - self.frame_from
         ms = (ctypes.c_double * n)()
         d = self.directory if self.directory.endswith(os.sep) or not self.directory else self.directory + os.sep
-        flags = (N.FILES_WRITE_OBJ if self._save_obj else 0) | (N.FILES_SIDECAR if self._sidecar else 0)
+        flags = (N.FILES_WRITE_OBJ if self._save_obj else 0) | (N.FILES_SIDECAR if self._sidecar else 0) | \
+            (N.FILES_INDEXED_OBJ if self._indexed else 0)
         tm = N.FilesTiming()
         st = N.lib.fsr_reconstruct_files_ex(self._rec._h, d.encode(), self.file_pattern.encode(),
                                             self.frame_from, self.frame_to, flags, ms, ctypes.byref(tm))

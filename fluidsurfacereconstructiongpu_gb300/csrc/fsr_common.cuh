@@ -44,7 +44,8 @@ struct Counters {
     uint32_t need_mesh;
     uint32_t work_field;     // next window group of the anisotropic field (dynamic scheduling)
     uint32_t work_adjoint;   // the same for its adjoint
-    uint32_t pad[3];
+    uint32_t n_weld;         // welded mesh vertices (FSR_FLAG_WELD)
+    uint32_t pad[2];
 };
 
 // Rank directory over the band bitset: rank(v) = number of band vertices

@@ -74,6 +74,8 @@ struct fsr_handle {
     fsr::DevBuf sv, phi, mc, vofs, qpos, valid;
     // mesh
     fsr::DevBuf mesh_pos, mesh_nrm;
+    // vertex welding (FSR_FLAG_WELD)
+    fsr::DevBuf wkey, wslot, wrank, widx, wpos, wnrm, wtable_keys, wtable_first;
     fsr::DevBuf ctr;
     // backward pass
     fsr::DevBuf mv;                      // ZB05/Akinci12: per band vertex (mean - v, weight sum)

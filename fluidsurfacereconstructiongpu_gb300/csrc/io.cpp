@@ -363,13 +363,19 @@ fsr_status fsr_read_xyz_binary(const char* path, fsr_frame_header* hdr, float** 
     return read_xyzb(path, hdr, xyz, density, n, nullptr);
 }
 
-fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm, uint64_t nv)
+}  // extern "C"
+
+namespace {
+
+// v lines, vn lines, then f lines (face(w, t) writes triangle t's line),
+// formatted in blocks of lines by all threads into per-part buffers and
+// written in order.
+template <class Face>
+fsr_status write_obj_lines(const char* path, const float* pos, const float* nrm, uint64_t nv, uint64_t ntri,
+                           Face&& face)
 {
-    if (!path || (nv && (!pos || !nrm)) || nv % 3 != 0) return FSR_ERR_INVALID_ARGUMENT;
     FILE* f = std::fopen(path, "wb");
     if (!f) return FSR_ERR_IO;
-    // v lines, vn lines, f lines; formatted in blocks of lines by all
-    // threads into per-part buffers, written in order
     constexpr uint64_t kLines = 1 << 15;  // lines per part
     const uint32_t nt = io_threads();
     std::vector<std::vector<char>> out(nt);
@@ -403,24 +409,51 @@ fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm, u
     // "v x y z" / "vn x y z" with %g numbers (at most 15 characters each)
     emit(nv, 64, [&](char* w, uint64_t i) { return vec3(w, "v ", 2, pos + 3 * i); });
     emit(nv, 64, [&](char* w, uint64_t i) { return vec3(w, "vn ", 3, nrm + 3 * i); });
-    // "f a//a b//b c//c " per triangle, 1-based
-    emit(nv / 3, 2 + 6 * 22 + 8, [&](char* w, uint64_t t) {
-        *w++ = 'f';
-        *w++ = ' ';
-        for (uint64_t c = 0; c < 3; ++c) {
-            const uint64_t id = 3 * t + c + 1;
-            w = put_u(w, id);
-            *w++ = '/';
-            *w++ = '/';
-            w = put_u(w, id);
-            *w++ = ' ';
-        }
-        *w++ = '\n';
-        return w;
-    });
+    emit(ntri, 2 + 6 * 22 + 8, face);
     ok = std::fclose(f) == 0 && ok;
     return ok ? FSR_OK : FSR_ERR_IO;
 }
+
+// "f a//a b//b c//c " with 1-based vertex numbers
+inline char* face_line(char* w, uint64_t a, uint64_t b, uint64_t c)
+{
+    *w++ = 'f';
+    *w++ = ' ';
+    const uint64_t id[3] = {a, b, c};
+    for (int k = 0; k < 3; ++k) {
+        w = put_u(w, id[k]);
+        *w++ = '/';
+        *w++ = '/';
+        w = put_u(w, id[k]);
+        *w++ = ' ';
+    }
+    *w++ = '\n';
+    return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm, uint64_t nv)
+{
+    if (!path || (nv && (!pos || !nrm)) || nv % 3 != 0) return FSR_ERR_INVALID_ARGUMENT;
+    return write_obj_lines(path, pos, nrm, nv, nv / 3,
+                           [](char* w, uint64_t t) { return face_line(w, 3 * t + 1, 3 * t + 2, 3 * t + 3); });
+}
+
+fsr_status fsr_write_obj_indexed(const char* path, const float* pos, const float* nrm, uint64_t nv,
+                                 const uint32_t* idx, uint64_t ni)
+{
+    if (!path || (nv && (!pos || !nrm)) || (ni && !idx) || ni % 3 != 0) return FSR_ERR_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < ni; ++i)
+        if (idx[i] >= nv) return FSR_ERR_INVALID_ARGUMENT;
+    return write_obj_lines(path, pos, nrm, nv, ni / 3, [idx](char* w, uint64_t t) {
+        return face_line(w, (uint64_t)idx[3 * t] + 1, (uint64_t)idx[3 * t + 1] + 1, (uint64_t)idx[3 * t + 2] + 1);
+    });
+}
+
+}  // extern "C"
 
 namespace {
 
@@ -469,6 +502,8 @@ LoadedFrame load_frame(const std::string& stem, bool sidecar)
 }
 
 }  // namespace
+
+extern "C" {
 
 fsr_status fsr_reconstruct_files_ex(fsr_handle* h, const char* directory, const char* pattern, uint32_t from,
                                     uint32_t to, uint32_t flags, double* frame_ms, fsr_files_timing* timing)
@@ -523,10 +558,14 @@ fsr_status fsr_reconstruct_files_ex(fsr_handle* h, const char* directory, const 
         tm.reconstruct_ms += ms;
         if (frame_ms) frame_ms[fr - from] = ms;
         if (flags & FSR_FILES_WRITE_OBJ) {
-            uint64_t nv = h->stats.n_mesh_vertices;
+            const bool indexed = (flags & FSR_FILES_INDEXED_OBJ) != 0;
+            uint64_t nv = indexed ? h->stats.n_weld_vertices : h->stats.n_mesh_vertices;
+            uint64_t ni = indexed ? h->stats.n_mesh_vertices : 0;
             auto mp = std::make_shared<std::vector<float>>(3 * nv);
             auto mn = std::make_shared<std::vector<float>>(3 * nv);
-            st = fsr_copy_mesh(h, mp->data(), mn->data(), nv, &nv);
+            auto mi = std::make_shared<std::vector<uint32_t>>(ni);
+            st = indexed ? fsr_copy_indexed_mesh(h, mp->data(), mn->data(), nv, mi->data(), ni, &nv, &ni)
+                         : fsr_copy_mesh(h, mp->data(), mn->data(), nv, &nv);
             if (st != FSR_OK) break;
             if (writer.valid()) {
                 st = writer.get();
@@ -536,9 +575,11 @@ fsr_status fsr_reconstruct_files_ex(fsr_handle* h, const char* directory, const 
                 }
             }
             writer_path = stem + ".obj";
-            writer = std::async(std::launch::async, [mp, mn, nv, path = writer_path, &write_ms]() {
+            writer = std::async(std::launch::async, [mp, mn, mi, nv, ni, indexed, path = writer_path, &write_ms]() {
                 const auto a = std::chrono::steady_clock::now();
-                const fsr_status s = fsr_write_obj(path.c_str(), mp->data(), mn->data(), nv);
+                const fsr_status s = indexed
+                                         ? fsr_write_obj_indexed(path.c_str(), mp->data(), mn->data(), nv, mi->data(), ni)
+                                         : fsr_write_obj(path.c_str(), mp->data(), mn->data(), nv);
                 write_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
                 return s;
             });

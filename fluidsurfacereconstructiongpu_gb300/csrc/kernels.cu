@@ -758,6 +758,18 @@ __global__ void k_mc_generate(McArgs a, const Counters* ctr)
             a.out_nrm[o] = sgn * nx;
             a.out_nrm[o + 1] = sgn * ny;
             a.out_nrm[o + 2] = sgn * nz;
+            if (a.out_key) {
+                // the edge's lower end point and its axis (the one coordinate
+                // in which the two corners differ)
+                const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
+                const uint32_t lx = x + (uint32_t)min(mc::cornerDx(i0), mc::cornerDx(i1));
+                const uint32_t ly = y + (uint32_t)min(mc::cornerDy(i0), mc::cornerDy(i1));
+                const uint32_t lz = z + (uint32_t)min(mc::cornerDz(i0), mc::cornerDz(i1));
+                const uint32_t axis = mc::cornerDx(i0) != mc::cornerDx(i1) ? 0u
+                                      : (mc::cornerDy(i0) != mc::cornerDy(i1) ? 1u : 2u);
+                const uint64_t lin = (uint64_t)lx + (uint64_t)a.sc.res[0] * ((uint64_t)ly + (uint64_t)a.sc.res[1] * lz);
+                a.out_key[base + k] = 3ull * lin + axis;
+            }
         }
     }
 }

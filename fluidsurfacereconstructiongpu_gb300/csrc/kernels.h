@@ -135,6 +135,7 @@ struct McArgs {
     uint32_t* valid;       // valid cube list (positions in sv)
     float* out_pos;
     float* out_nrm;
+    uint64_t* out_key;     // may be null: per mesh vertex, its grid edge (3 x lower end point + axis)
     float iso, fill;
     int host_mc;           // Akinci12: the host marching cubes' normal/lerp rules
     uint32_t cap_band, cap_valid, cap_mesh;
@@ -148,6 +149,26 @@ void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint
                            const uint8_t* psurf, uint32_t n, uint32_t* out);
 
 void upload_mc_tables(cudaStream_t s);
+
+// Vertex welding of the triangle soup (weld.cu).
+struct WeldArgs {
+    const uint64_t* keys;  // per soup vertex: its grid edge (McArgs::out_key)
+    const float* pos;      // soup positions and normals, 3 floats per vertex
+    const float* nrm;
+    uint32_t cap;          // soup capacity (the mesh pool)
+    uint64_t* table_keys;  // hash table: table_size keys and first occurrences
+    uint32_t* table_first;
+    uint32_t table_size;   // power of two, >= 2 cap (weld_table_size)
+    uint32_t shift;        // set by launch_weld
+    uint32_t* slot;        // per soup vertex: its table slot
+    uint32_t* rank;        // per soup vertex: first-occurrence flag, then its number
+    uint32_t* index;       // out: per soup vertex, its welded vertex
+    float* out_pos;        // out: welded positions and normals (first occurrences)
+    float* out_nrm;
+};
+uint32_t weld_table_size(uint32_t cap);
+// Queues the weld; the welded vertex count lands in ctr->n_weld.
+cudaError_t launch_weld(const KernelCtx& c, WeldArgs a, Counters* ctr, uint32_t* scan_scratch);
 
 // Number of kernels launched by this thread through the wrappers (the
 // frame's gpu_launches figure).

@@ -173,7 +173,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -242,7 +242,20 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         CK(cudaEventCreate(&h->ev_start));
         for (auto& e : h->ev) CK(cudaEventCreate(&e));
     }
-    const uint64_t scan_words = std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
+    const bool weld = (p.flags & FSR_FLAG_WELD) != 0;
+    uint64_t scan_words = std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
+    if (weld) {
+        scan_words = std::max<uint64_t>(scan_words, scan_scratch_words(h->cap_mesh));
+        const uint64_t cm = h->cap_mesh, ts = weld_table_size(h->cap_mesh);
+        CK(h->wkey.ensure(8 * cm));
+        CK(h->wslot.ensure(4 * cm));
+        CK(h->wrank.ensure(4 * cm));
+        CK(h->widx.ensure(4 * cm));
+        CK(h->wpos.ensure(12 * cm));
+        CK(h->wnrm.ensure(12 * cm));
+        CK(h->wtable_keys.ensure(8 * ts));
+        CK(h->wtable_first.ensure(4 * ts));
+    }
     CK(h->scan_tmp.ensure(4ull * scan_words));
     CK(h->sv.ensure(4ull * h->cap_band));
     CK(h->phi.ensure(4ull * h->cap_band));
@@ -407,6 +420,8 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     ma.cap_band = h->cap_band;
     ma.cap_valid = h->cap_valid;
     ma.cap_mesh = h->cap_mesh;
+    const bool weld = (p.flags & FSR_FLAG_WELD) != 0;
+    ma.out_key = weld ? (uint64_t*)h->wkey.ptr : nullptr;
     launch_mc_classify(kc, ma, ctr);
     mark(8);
     CK(scan_u32(ma.mc, (uint32_t*)h->vofs.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_mesh_verts,
@@ -416,6 +431,22 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     launch_valid_list(kc, ma, ctr);
     mark(9);
     launch_mc_generate(kc, ma, ctr);
+    if (weld) {
+        WeldArgs wa{};
+        wa.keys = (const uint64_t*)h->wkey.ptr;
+        wa.pos = (const float*)h->mesh_pos.ptr;
+        wa.nrm = (const float*)h->mesh_nrm.ptr;
+        wa.cap = h->cap_mesh;
+        wa.table_keys = (uint64_t*)h->wtable_keys.ptr;
+        wa.table_first = (uint32_t*)h->wtable_first.ptr;
+        wa.table_size = weld_table_size(h->cap_mesh);
+        wa.slot = (uint32_t*)h->wslot.ptr;
+        wa.rank = (uint32_t*)h->wrank.ptr;
+        wa.index = (uint32_t*)h->widx.ptr;
+        wa.out_pos = (float*)h->wpos.ptr;
+        wa.out_nrm = (float*)h->wnrm.ptr;
+        CK(launch_weld(kc, wa, ctr, (uint32_t*)h->scan_tmp.ptr));
+    }
     mark(10);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->pinned_ctr, ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -453,6 +484,7 @@ fsr_status frame_finish(fsr_handle* h, const FramePlan& fp, bool timing, bool* r
     s.n_band_vertices = hc.n_band;
     s.n_valid_cubes = hc.n_valid;
     s.n_mesh_vertices = hc.n_mesh_verts;
+    s.n_weld_vertices = (h->params.flags & FSR_FLAG_WELD) ? hc.n_weld : 0;
     s.n_fp64_fallbacks = hc.n_fp64;
     s.n_kernel_launches = h->launches_frame;
     s.n_backward_launches = 0;
@@ -650,6 +682,26 @@ fsr_status fsr_copy_mesh(fsr_handle* h, float* out_pos, float* out_nrm, uint64_t
     return FSR_OK;
 }
 
+fsr_status fsr_copy_indexed_mesh(fsr_handle* h, float* pos, float* nrm, uint64_t vertex_capacity, uint32_t* indices,
+                                 uint64_t index_capacity, uint64_t* n_vertices, uint64_t* n_indices)
+{
+    if (!h || !n_vertices || !n_indices) return FSR_ERR_INVALID_ARGUMENT;
+    if (!h->frame_ready) return fail(h, FSR_ERR_NOT_READY, "no frame reconstructed");
+    if (!(h->params.flags & FSR_FLAG_WELD)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "FSR_FLAG_WELD is not set");
+    DeviceGuard g(h->device);
+    const uint64_t nv = h->stats.n_weld_vertices, ni = h->stats.n_mesh_vertices;
+    *n_vertices = nv;
+    *n_indices = ni;
+    if (nv > vertex_capacity || ni > index_capacity) return fail(h, FSR_ERR_CAPACITY, "indexed mesh buffers too small");
+    if (nv) {
+        if (!pos || !nrm || !indices) return FSR_ERR_INVALID_ARGUMENT;
+        CK(cudaMemcpy(pos, h->wpos.ptr, 12ull * nv, cudaMemcpyDefault));
+        CK(cudaMemcpy(nrm, h->wnrm.ptr, 12ull * nv, cudaMemcpyDefault));
+        CK(cudaMemcpy(indices, h->widx.ptr, 4ull * ni, cudaMemcpyDefault));
+    }
+    return FSR_OK;
+}
+
 fsr_status fsr_get_stats(const fsr_handle* h, fsr_stats* out)
 {
     if (!h || !out) return FSR_ERR_INVALID_ARGUMENT;
@@ -688,6 +740,7 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
     case FSR_DBG_MEAN:
     case FSR_DBG_SMOOTHED: need = yu13 ? 12 * n : 0; break;
     case FSR_DBG_G: need = yu13 ? 36 * n : 0; break;
+    case FSR_DBG_WELD_KEYS: need = (h->params.flags & FSR_FLAG_WELD) ? 8 * s.n_mesh_vertices : 0; break;
     default: return fail(h, FSR_ERR_INVALID_ARGUMENT, "unknown debug array %u", which);
     }
     if (bytes_needed) *bytes_needed = need;
@@ -728,6 +781,7 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
         break;
     }
     case FSR_DBG_VALID_CUBES: CK(cudaMemcpy(dst, h->valid.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_WELD_KEYS: CK(cudaMemcpy(dst, h->wkey.ptr, need, cudaMemcpyDeviceToHost)); break;
     case FSR_DBG_MEAN: CK(copy4(h->mean, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_SMOOTHED: CK(copy4(h->smoothed, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_G: {

@@ -71,6 +71,13 @@ typedef struct fsr_params {
  * instead of 2^20 (they grow on demand, re-running the frame once): for
  * memory-tight callers and batches of many small frames. */
 #define FSR_FLAG_SMALL_POOLS 0x4u
+/* Weld the triangle soup into an indexed mesh at the end of every frame
+ * (fsr_copy_indexed_mesh).  The soup's vertices sit on scalar-grid edges
+ * (generateTriangles, ReconstructionCUDA.cu:383-463, three unshared vertices
+ * per triangle); the copies of one edge's vertex become one mesh vertex,
+ * numbered in order of first use, with the position and normal of that first
+ * copy.  The soup itself is unchanged. */
+#define FSR_FLAG_WELD 0x8u
 
 /* The .xyz header (data_format.txt:1-15; ReconstructorGPU.cpp:215-251). */
 typedef struct fsr_frame_header {
@@ -101,6 +108,7 @@ typedef struct fsr_stats {
     float stage_ms[FSR_NUM_STAGES];/* with FSR_FLAG_STAGE_TIMING */
     float total_ms;
     uint64_t device_bytes;         /* device memory held by the handle's pools */
+    uint64_t n_weld_vertices;      /* with FSR_FLAG_WELD: vertices of the indexed mesh */
 } fsr_stats;
 
 typedef struct fsr_handle fsr_handle;
@@ -142,6 +150,15 @@ fsr_status fsr_mesh_device(fsr_handle* h, const float** d_pos, const float** d_n
 fsr_status fsr_copy_mesh(fsr_handle* h, float* out_pos, float* out_nrm, uint64_t capacity,
                          uint64_t* n_vertices);
 
+/* The last frame's welded mesh (FSR_FLAG_WELD): n_vertices positions and
+ * normals (3 floats each) and one index per soup vertex (n_indices = 3 x
+ * triangles, the soup's triangle order).  Host or device buffers.  If either
+ * count exceeds its capacity nothing is copied and FSR_ERR_CAPACITY is
+ * returned with both counts set. */
+fsr_status fsr_copy_indexed_mesh(fsr_handle* h, float* pos, float* nrm, uint64_t vertex_capacity,
+                                 uint32_t* indices, uint64_t index_capacity, uint64_t* n_vertices,
+                                 uint64_t* n_indices);
+
 /* Device-to-device copy of the last frame's mesh into caller buffers
  * (either pointer may be NULL); queued on `stream`. */
 fsr_status fsr_copy_mesh_device(fsr_handle* h, float* d_pos, float* d_nrm, uint64_t capacity,
@@ -179,7 +196,9 @@ typedef enum fsr_debug_array {
     FSR_DBG_VALID_CUBES = 8,     /* u32[Q]  positions in the band list of valid cubes */
     FSR_DBG_MEAN = 9,            /* f32[N*3] Yu13 weighted means (sorted order) */
     FSR_DBG_SMOOTHED = 10,       /* f32[N*3] Yu13 smoothed positions */
-    FSR_DBG_G = 11               /* f32[N*9] Yu13 G matrices, row-major, sorted order (*) */
+    FSR_DBG_G = 11,              /* f32[N*9] Yu13 G matrices, row-major, sorted order (*) */
+    FSR_DBG_WELD_KEYS = 12       /* u64[3T] grid edge of each soup vertex, 3 x lower end point + axis
+                                    (with FSR_FLAG_WELD) */
 } fsr_debug_array;
 
 fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes,
@@ -308,6 +327,12 @@ void fsr_free_host(void* p);
 fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm,
                          uint64_t n_vertices);
 
+/* Writes an indexed mesh as .obj: one v and one vn line per vertex, then
+ * "f a//a b//b c//c " per triangle with 1-based indices (the layout of
+ * fsr_write_obj with shared vertices). */
+fsr_status fsr_write_obj_indexed(const char* path, const float* pos, const float* nrm, uint64_t n_vertices,
+                                 const uint32_t* indices, uint64_t n_indices);
+
 /* Host threads of fsr_read_xyz and fsr_write_obj (0, the default: one per
  * core, at most 64). */
 void fsr_io_set_threads(uint32_t n);
@@ -337,6 +362,9 @@ fsr_status fsr_reconstruct_files(fsr_handle* h, const char* directory, const cha
  * the .xyz as it is now (same size and modification time); after parsing an
  * .xyz, write its sidecar (best effort). */
 #define FSR_FILES_SIDECAR 0x2u
+/* Write the welded mesh (fsr_write_obj_indexed) instead of the soup; the
+ * handle must have FSR_FLAG_WELD. */
+#define FSR_FILES_INDEXED_OBJ 0x4u
 
 /* Host milliseconds of a file-driven run, summed over its frames.  Reading
  * and writing overlap the GPU work (frame k + 1 is read and frame k - 1's

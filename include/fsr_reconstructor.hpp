@@ -71,7 +71,8 @@ public:
         std::vector<double> tri, spr, svr, es, sf, mc;
         for (unsigned int f = mFrom; f < mTo; ++f) {
             double ms = 0.0;
-            const uint32_t flags = (mSaveObjFile ? FSR_FILES_WRITE_OBJ : 0u) | (mSidecar ? FSR_FILES_SIDECAR : 0u);
+            const uint32_t flags = (mSaveObjFile ? FSR_FILES_WRITE_OBJ : 0u) | (mSidecar ? FSR_FILES_SIDECAR : 0u) |
+                                   (mIndexed ? FSR_FILES_INDEXED_OBJ : 0u);
             check(fsr_reconstruct_files_ex(mHandle, mDirectory.c_str(), mPattern.c_str(), f, f + 1, flags, &ms,
                                            nullptr),
                   "frame " + std::to_string(f));
@@ -100,6 +101,14 @@ public:
     /* Read stem.xyzb instead of parsing stem.xyz when it is current, and
      * write it after parsing (FSR_FILES_SIDECAR). */
     void setBinarySidecar(bool flag) { mSidecar = flag; }
+    /* Write welded (indexed) .obj files instead of triangle soups
+     * (FSR_FLAG_WELD, FSR_FILES_INDEXED_OBJ). */
+    void setIndexedMesh(bool flag)
+    {
+        mIndexed = flag;
+        mParams.flags = flag ? (mParams.flags | FSR_FLAG_WELD) : (mParams.flags & ~FSR_FLAG_WELD);
+        if (mHandle) check(fsr_set_params(mHandle, &mParams), "fsr_set_params");
+    }
 
     SimParam getSimulationParameters() const
     {
@@ -169,7 +178,7 @@ protected:
     std::string mDirectory, mPattern;
     unsigned int mFrom, mTo;
     int mDevice;
-    bool mSaveObjFile = true, mSaveVisFile = false, mSaveCfgFile = false, mSidecar = false;
+    bool mSaveObjFile = true, mSaveVisFile = false, mSaveCfgFile = false, mSidecar = false, mIndexed = false;
     fsr_params mParams{};
     fsr_handle* mHandle = nullptr;
     fsr_frame_header mHeader{};
