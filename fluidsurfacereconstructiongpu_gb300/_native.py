@@ -79,6 +79,7 @@ BATCH_NO_AUTOTUNE = 0x2
 FILES_WRITE_OBJ = 0x1
 FILES_SIDECAR = 0x2
 FILES_INDEXED_OBJ = 0x4
+FILES_WRITE_VIS = 0x8
 
 
 class FilesTiming(ctypes.Structure):
@@ -126,6 +127,7 @@ def _load():
         "fsr_io_set_threads": (None, [c_u32]),
         "fsr_copy_indexed_mesh": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, c_vp, c_u64, P(c_u64), P(c_u64)]),
         "fsr_write_obj_indexed": (ctypes.c_int, [ctypes.c_char_p, c_vp, c_vp, c_u64, c_vp, c_u64]),
+        "fsr_write_vis": (ctypes.c_int, [c_vp, ctypes.c_char_p, ctypes.c_char_p]),
         "fsr_write_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), c_vp, c_vp, c_u64]),
         "fsr_read_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
     }

@@ -196,6 +196,11 @@ class Reconstructor:
         N.check(N.lib.fsr_get_stats(self._h, ctypes.byref(s)), self._h)
         return s
 
+    def write_vis(self, path: str, mesh_name: str) -> None:
+        """The last frame's intermediates as a .vis file (the reference
+        viewer's debug dump); mesh_name is recorded as its mesh file."""
+        N.check(N.lib.fsr_write_vis(self._h, path.encode(), mesh_name.encode()), self._h)
+
     def indexed_mesh(self) -> "IndexedMesh":
         """The last frame's welded mesh (needs weld=True)."""
         s = self.stats()
@@ -394,6 +399,7 @@ class ReconstructorGPU:
         self._num_particles = 0
         self._sidecar = False
         self._indexed = False
+        self._save_vis = False
         self._io = None
 
     def getAlgorithmType(self) -> str:
@@ -406,8 +412,7 @@ class ReconstructorGPU:
         self._save_cfg = bool(flag)
 
     def setOutputVisualizeFile(self, flag: bool):
-        if flag:
-            raise NotImplementedError(".vis debug dumps are not produced by this library")
+        self._save_vis = bool(flag)
 
     def setIndexedMesh(self, flag: bool):
         """Write welded (indexed) .obj files instead of triangle soups."""
@@ -441,7 +446,7 @@ class ReconstructorGPU:
         ms = (ctypes.c_double * n)()
         d = self.directory if self.directory.endswith(os.sep) or not self.directory else self.directory + os.sep
         flags = (N.FILES_WRITE_OBJ if self._save_obj else 0) | (N.FILES_SIDECAR if self._sidecar else 0) | \
-            (N.FILES_INDEXED_OBJ if self._indexed else 0)
+            (N.FILES_INDEXED_OBJ if self._indexed else 0) | (N.FILES_WRITE_VIS if self._save_vis else 0)
         tm = N.FilesTiming()
         st = N.lib.fsr_reconstruct_files_ex(self._rec._h, d.encode(), self.file_pattern.encode(),
                                             self.frame_from, self.frame_to, flags, ms, ctypes.byref(tm))

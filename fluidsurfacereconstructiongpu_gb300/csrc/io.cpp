@@ -557,6 +557,16 @@ fsr_status fsr_reconstruct_files_ex(fsr_handle* h, const char* directory, const 
         const double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         tm.reconstruct_ms += ms;
         if (frame_ms) frame_ms[fr - from] = ms;
+        if (flags & FSR_FILES_WRITE_VIS) {
+            // after the timed scope, as ReconstructorGPU::reconstruct does (cpp:57-61)
+            char base[512];
+            std::snprintf(base, sizeof(base), pattern, fr);
+            st = fsr_write_vis(h, (stem + ".vis").c_str(), (std::string(base) + ".obj").c_str());
+            if (st != FSR_OK) {
+                if (h->last_error.empty()) h->last_error = "cannot write " + stem + ".vis";
+                break;
+            }
+        }
         if (flags & FSR_FILES_WRITE_OBJ) {
             const bool indexed = (flags & FSR_FILES_INDEXED_OBJ) != 0;
             uint64_t nv = indexed ? h->stats.n_weld_vertices : h->stats.n_mesh_vertices;

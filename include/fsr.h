@@ -333,6 +333,17 @@ fsr_status fsr_write_obj(const char* path, const float* pos, const float* nrm,
 fsr_status fsr_write_obj_indexed(const char* path, const float* pos, const float* nrm, uint64_t n_vertices,
                                  const uint32_t* indices, uint64_t n_indices);
 
+/* Writes the last frame's intermediates as a .vis file, the debug dump the
+ * reference's viewer reads (saveMiddleDataToVisFile:
+ * ReconstructorGPUOursZB05.cpp:104-230, ReconstructorGPUOursYu13.cpp:285-420,
+ * ReconstructorGPUAkinci12.cpp:290-420), same layout and number format:
+ * both grids (min, max, resolution, cell size), the particle radius, the
+ * particles in cell order, the occupied cells, the smoothed particles (Yu13;
+ * 0 otherwise), the band vertices, the surface particles, the involved
+ * particles (Yu13; 0 otherwise), the valid cubes (positions in the band
+ * list), `mesh_name` and the kernel radius h. */
+fsr_status fsr_write_vis(fsr_handle* h, const char* path, const char* mesh_name);
+
 /* Host threads of fsr_read_xyz and fsr_write_obj (0, the default: one per
  * core, at most 64). */
 void fsr_io_set_threads(uint32_t n);
@@ -365,6 +376,8 @@ fsr_status fsr_reconstruct_files(fsr_handle* h, const char* directory, const cha
 /* Write the welded mesh (fsr_write_obj_indexed) instead of the soup; the
  * handle must have FSR_FLAG_WELD. */
 #define FSR_FILES_INDEXED_OBJ 0x4u
+/* Write stem.vis per frame (fsr_write_vis; setOutputVisualizeFile). */
+#define FSR_FILES_WRITE_VIS 0x8u
 
 /* Host milliseconds of a file-driven run, summed over its frames.  Reading
  * and writing overlap the GPU work (frame k + 1 is read and frame k - 1's

@@ -18,9 +18,11 @@
  * ReconstructorGPU.cpp:339-395 (triangles, surface-particle ratio,
  * surface-vertex ratio, then four stage-time sums in milliseconds).
  *
+ * setOutputVisualizeFile writes each frame's .vis dump (fsr_write_vis).
+ *
  * Differences: errors throw fsr_gb300::Error instead of printing and exiting
- * the process; the .vis visualisation dump (setOutputVisualizeFile) is not
- * written (the viewer is not part of this library), the flag is kept.
+ * the process.  Extensions: setBinarySidecar (.xyzb) and setIndexedMesh
+ * (welded .obj).
  */
 #ifndef FSR_RECONSTRUCTOR_HPP
 #define FSR_RECONSTRUCTOR_HPP
@@ -72,7 +74,7 @@ public:
         for (unsigned int f = mFrom; f < mTo; ++f) {
             double ms = 0.0;
             const uint32_t flags = (mSaveObjFile ? FSR_FILES_WRITE_OBJ : 0u) | (mSidecar ? FSR_FILES_SIDECAR : 0u) |
-                                   (mIndexed ? FSR_FILES_INDEXED_OBJ : 0u);
+                                   (mIndexed ? FSR_FILES_INDEXED_OBJ : 0u) | (mSaveVisFile ? FSR_FILES_WRITE_VIS : 0u);
             check(fsr_reconstruct_files_ex(mHandle, mDirectory.c_str(), mPattern.c_str(), f, f + 1, flags, &ms,
                                            nullptr),
                   "frame " + std::to_string(f));
