@@ -407,6 +407,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-backward", action="store_true", help="skip the forward+backward leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames leg")
+    ap.add_argument("--compute-density", action="store_true",
+                    help="frames without densities: the GPU computes them (FSR_FLAG_COMPUTE_DENSITY); "
+                         "no backward or batch legs")
     ap.add_argument("--io", action="store_true",
                     help="time the file-driven loop (.xyz in, .obj out) instead of the in-memory frame")
     args = ap.parse_args()
@@ -415,6 +418,9 @@ def main():
     if args.io:
         run_io_leg(args, w)
         return
+    if args.compute_density:
+        args.no_backward = True
+        args.no_batch = True
 
     if args.impl == "reference":
         fr = make_frame(w)
@@ -437,10 +443,11 @@ def main():
         s, label, threads, sample = cpu_frame(w, fr, args.cpu_field_stride)
         cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample}
 
-    rec = api.Reconstructor(w["method"], local, stage_timing=True, **recon_kwargs(w))
+    rec = api.Reconstructor(w["method"], local, stage_timing=True, compute_density=args.compute_density,
+                            **recon_kwargs(w))
     hdr = api.header_of(fr)
     xyz = torch.from_numpy(fr.pos).to(dev)
-    den = torch.from_numpy(fr.density).to(dev)
+    den = None if args.compute_density else torch.from_numpy(fr.density).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
     launches0 = None
@@ -533,7 +540,8 @@ def main():
         flush.zero_()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        rc = _native.lib.fsr_reconstruct_host(rec._h, ctypes.byref(hdr), pin_xyz.data_ptr(), pin_den.data_ptr(),
+        rc = _native.lib.fsr_reconstruct_host(rec._h, ctypes.byref(hdr), pin_xyz.data_ptr(),
+                                              None if args.compute_density else pin_den.data_ptr(),
                                               fr.n, out_pos.data_ptr(), out_nrm.data_ptr(), cap,
                                               ctypes.byref(nvo), ctypes.c_void_p(stream.cuda_stream))
         _native.check(rc, rec._h)
@@ -541,7 +549,7 @@ def main():
         if k >= args.warmup:
             e2e_t.append(t1 - t0)
     e2e_step = float(np.mean(e2e_t))
-    h2d = fr.n * 16
+    h2d = fr.n * (12 if args.compute_density else 16)
     d2h = int(nvo.value) * 24 + 64
 
     # roofline of the dominant kernel (the field stage)
@@ -564,6 +572,7 @@ def main():
                        "band_vertices": B, "triangles": int(st.n_mesh_vertices) // 3,
                        "device_bytes": int(rec.stats().device_bytes), "fp64_fallbacks": int(st.n_fp64_fallbacks),
                        "scalar_grid": list(st.scalar_res), "l2": "flushed (256 MB write) between steps",
+                       "densities": "computed on the GPU (SPH, poly6)" if args.compute_density else "input",
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": fr.n / e2e_step, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

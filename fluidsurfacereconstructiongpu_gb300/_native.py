@@ -27,9 +27,10 @@ FLAG_KEEP_INTERMEDIATES = 0x1
 FLAG_STAGE_TIMING = 0x2
 FLAG_SMALL_POOLS = 0x4
 FLAG_WELD = 0x8
+FLAG_COMPUTE_DENSITY = 0x10
 
 DBG = dict(perm=0, sorted_xyz=1, ranges=2, surface_flags=3, involved_counts=4, band=5, field=6,
-           mc_info=7, valid=8, mean=9, smoothed=10, G=11, weld_keys=12)
+           mc_info=7, valid=8, mean=9, smoothed=10, G=11, weld_keys=12, density=13)
 
 NUM_STAGES = 12
 STAGE_NAMES = ["hash+sort", "ranges", "surface", "band stamp", "band list", "smoothing", "covariance",

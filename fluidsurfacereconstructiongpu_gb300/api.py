@@ -71,7 +71,7 @@ class Reconstructor:
                  grid_ratio: Optional[int] = None, cell_size_scale: Optional[float] = None,
                  smoothing_lambda: Optional[float] = None, aniso_radius_over_h: Optional[float] = None,
                  min_neighbors: Optional[int] = None, keep_intermediates: bool = False,
-                 stage_timing: bool = False, weld: bool = False):
+                 stage_timing: bool = False, weld: bool = False, compute_density: bool = False):
         self.method = method
         p = default_params(method)
         if iso is not None:
@@ -87,7 +87,8 @@ class Reconstructor:
         if min_neighbors is not None:
             p.min_neighbors = min_neighbors
         p.flags = (N.FLAG_KEEP_INTERMEDIATES if keep_intermediates else 0) | \
-            (N.FLAG_STAGE_TIMING if stage_timing else 0) | (N.FLAG_WELD if weld else 0)
+            (N.FLAG_STAGE_TIMING if stage_timing else 0) | (N.FLAG_WELD if weld else 0) | \
+            (N.FLAG_COMPUTE_DENSITY if compute_density else 0)
         self.params = p
         h = ctypes.c_void_p()
         st = N.lib.fsr_create(ctypes.byref(p), int(device), ctypes.byref(h))
@@ -115,17 +116,22 @@ class Reconstructor:
 
     # -- frames
     def reconstruct(self, xyz, density, header: N.FrameHeader, stream=None) -> int:
-        """Device path: xyz (N,3) and density (N,) float32 CUDA tensors.
-        Returns the number of mesh vertices; the mesh stays on the device."""
+        """Device path: xyz (N,3) and density (N,) float32 CUDA tensors
+        (density may be None with compute_density=True).  Returns the number
+        of mesh vertices; the mesh stays on the device."""
         import torch
-        assert xyz.is_cuda and density.is_cuda, "device path needs CUDA tensors"
+        assert xyz.is_cuda and (density is None or density.is_cuda), "device path needs CUDA tensors"
         xyz = xyz.contiguous()
-        density = density.contiguous()
-        assert xyz.dtype == torch.float32 and density.dtype == torch.float32
-        n = int(density.numel())
+        assert xyz.dtype == torch.float32
+        n = int(xyz.numel() // 3)
+        dptr = None
+        if density is not None:
+            density = density.contiguous()
+            assert density.dtype == torch.float32 and int(density.numel()) == n
+            dptr = density.data_ptr()
         s = stream if stream is not None else torch.cuda.current_stream(xyz.device)
         st = N.lib.fsr_reconstruct(self._h, ctypes.byref(header), ctypes.c_void_p(xyz.data_ptr()),
-                                   ctypes.c_void_p(density.data_ptr()), n, ctypes.c_void_p(s.cuda_stream))
+                                   ctypes.c_void_p(dptr), n, ctypes.c_void_p(s.cuda_stream))
         N.check(st, self._h)
         return int(self.stats().n_mesh_vertices)
 
@@ -222,7 +228,7 @@ class Reconstructor:
             if need.value:
                 N.check(N.lib.fsr_debug_fetch(self._h, which, out.ctypes.data, need.value, None), self._h)
             return out
-        dtype = np.float32 if name in ("sorted_xyz", "field", "mean", "smoothed", "G") else np.uint32
+        dtype = np.float32 if name in ("sorted_xyz", "field", "mean", "smoothed", "G", "density") else np.uint32
         out = np.empty(need.value // 4, dtype=dtype)
         if need.value:
             N.check(N.lib.fsr_debug_fetch(self._h, which, out.ctypes.data, need.value, None), self._h)

@@ -49,6 +49,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
 {
     if (!h) return FSR_ERR_INVALID_ARGUMENT;
     if (!h->frame_ready) return bwd_fail(h, FSR_ERR_NOT_READY, "no frame reconstructed");
+    if (h->params.flags & FSR_FLAG_COMPUTE_DENSITY)
+        return bwd_fail(h, FSR_ERR_INVALID_ARGUMENT, "no backward pass for frames with computed densities");
     const uint64_t n = h->n_last;
     if (n > 0 && !d_grad_xyz) return bwd_fail(h, FSR_ERR_INVALID_ARGUMENT, "null gradient output");
     if (h->stats.n_mesh_vertices > 0 && !d_grad_mesh_pos)

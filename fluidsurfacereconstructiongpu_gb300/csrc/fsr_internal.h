@@ -66,6 +66,7 @@ struct fsr_handle {
     fsr::DevBuf mean, smoothed, grec;    // Yu13
     fsr::DevBuf covrec;                  // Yu13: normalised covariance, weight sum, neighbour-count flag
     fsr::DevBuf pflags;                  // u32 surface flags (debug)
+    fsr::DevBuf rho;                     // computed densities, sorted order (FSR_FLAG_COMPUTE_DENSITY)
     // cell-sized
     fsr::DevBuf ranges, occ, surf, invol, cell_rmax;
     // vertex-sized

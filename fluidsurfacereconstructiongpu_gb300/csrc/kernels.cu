@@ -86,7 +86,57 @@ __global__ void k_ranges_gather(const uint32_t* __restrict__ skeys, const uint32
     }
     if (key != next) ranges[key].y = k + 1;
     const uint32_t s = perm[k];
-    sorted[k] = make_float4(xyz[3ull * s], xyz[3ull * s + 1], xyz[3ull * s + 2], dens[s]);
+    // without densities (computed later by k_density) w is left at 0
+    sorted[k] = make_float4(xyz[3ull * s], xyz[3ull * s + 1], xyz[3ull * s + 2], dens ? dens[s] : 0.0f);
+}
+
+// SPH density of each sorted particle, for frames without a density column
+// (the reference's .xyz files carry the simulator's densities and the
+// reference computes none): rho_i = m sigma / h^3 sum_j (1 - |x_i - x_j|^2 /
+// h^2)^3 over the particles within h, i itself included, sigma = 315 /
+// (64 pi) - the poly6 kernel with the normalisation of the reference's own
+// field kernel (anisotropicW, cuh:294-310, at G = I / h).  Each particle's
+// sum runs over its window's cells in order, so results are deterministic.
+__global__ void __launch_bounds__(kThreads) k_density(const float4* __restrict__ sorted, uint32_t n,
+                                                      const uint2* __restrict__ ranges, Grid sp, int ext, float h,
+                                                      float h2, float inv_h2, float scale, float* __restrict__ rho)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4 p = sorted[t];
+    const Window w = narrow(window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
+                                   cell1(p.z, sp.min[2], sp.cs), ext, sp),
+                            p.x, p.y, p.z, cull_radius(h, sp.cs), sp);
+    float sum = 0.f;
+    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+            // the row's cells are contiguous in the sorted array
+            const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
+            uint32_t beg = kEmpty, end = 0;
+            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
+                const uint2 r = __ldg(&ranges[c0 + xx]);
+                if (r.x != kEmpty) {
+                    beg = min(beg, r.x);
+                    end = max(end, r.y);
+                }
+            }
+            for (uint32_t i = beg; i < end; ++i) {
+                const float4 q = __ldg(&sorted[i]);
+                const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (d2 < h2) {
+                    const float u = 1.0f - d2 * inv_h2;
+                    sum = fmaf(u * u, u, sum);
+                }
+            }
+        }
+    rho[t] = scale * sum;
+}
+
+__global__ void k_set_density(float4* __restrict__ sorted, const float* __restrict__ rho, uint32_t n)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) sorted[t].w = rho[t];
 }
 
 // ------------------------------------------------------------ surface
@@ -817,6 +867,19 @@ void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint3
     if (!n) return;
     k_ranges_gather<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, perm, n, xyz, dens, sorted, ranges, occ);
     ++g_launches;
+}
+
+void launch_density(const KernelCtx& c, float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp, float h,
+                    float mass, float* rho)
+{
+    if (n == 0) return;
+    const int ext = std::max(1, (int)std::ceil((double)h * 1.0001 / sp.cs + 1e-4));
+    const float h2 = h * h;
+    const float sigma = 315.0f / (64.0f * 3.1415926535898f);
+    const float scale = mass * sigma / (h * h * h);
+    k_density<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, ext, h, h2, 1.0f / h2, scale, rho);
+    k_set_density<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, rho, n);
+    g_launches += 2;
 }
 
 void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf)

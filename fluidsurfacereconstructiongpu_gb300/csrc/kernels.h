@@ -28,6 +28,11 @@ void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint3
                           const float* xyz, const float* dens, float4* sorted, uint2* ranges,
                           uint8_t* occ);
 
+// SPH (poly6) density of each sorted particle into sorted[].w (rho: n
+// floats of scratch); for frames without densities (FSR_FLAG_COMPUTE_DENSITY).
+void launch_density(const KernelCtx& c, float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp, float h,
+                    float mass, float* rho);
+
 void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf);
 void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, const uint8_t* surf,
                            uint8_t* invol);

@@ -173,7 +173,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -236,6 +236,7 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         CK(h->covrec.ensure(32ull * nn));
     }
     if (p.method == FSR_METHOD_AKINCI12) CK(h->psurf.ensure(nn));
+    if (p.flags & FSR_FLAG_COMPUTE_DENSITY) CK(h->rho.ensure(4ull * nn));
     if (keep) CK(h->pflags.ensure(4ull * nn));
     if (!h->pinned_ctr) CK(cudaMallocHost(&h->pinned_ctr, sizeof(Counters)));
     if (timing && !h->ev_start) {
@@ -314,7 +315,10 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     float4* sorted = (float4*)h->sorted.ptr;
     uint2* ranges = (uint2*)h->ranges.ptr;
     uint8_t* occ = (uint8_t*)h->occ.ptr;
-    launch_ranges_gather(kc, skeys, perm, n, d_xyz, d_den, sorted, ranges, occ);
+    const bool own_density = (p.flags & FSR_FLAG_COMPUTE_DENSITY) != 0;
+    launch_ranges_gather(kc, skeys, perm, n, d_xyz, own_density ? nullptr : d_den, sorted, ranges, occ);
+    if (own_density)
+        launch_density(kc, sorted, n, ranges, sp, hdr.kernel_radius, hdr.particle_mass, (float*)h->rho.ptr);
     mark(1);
 
     // ---- surface cells / particles
@@ -619,7 +623,9 @@ fsr_status fsr_reconstruct(fsr_handle* h, const fsr_frame_header* hdr, const flo
                            uint64_t n, void* stream)
 {
     if (!h || !hdr) return FSR_ERR_INVALID_ARGUMENT;
-    if (n > 0 && (!d_xyz || !d_density)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
+    const bool own_density = (h->params.flags & FSR_FLAG_COMPUTE_DENSITY) != 0;
+    if (n > 0 && (!d_xyz || (!d_density && !own_density)))
+        return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
     DeviceGuard g(h->device);
     h->frame_ready = false;
     return run_frame(h, *hdr, d_xyz, d_density, n, (cudaStream_t)stream);
@@ -630,7 +636,9 @@ fsr_status fsr_reconstruct_host(fsr_handle* h, const fsr_frame_header* hdr, cons
                                 void* stream)
 {
     if (!h || !hdr || !n_vertices) return FSR_ERR_INVALID_ARGUMENT;
-    if (n > 0 && (!xyz || !density)) return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
+    const bool own_density = (h->params.flags & FSR_FLAG_COMPUTE_DENSITY) != 0;
+    if (n > 0 && (!xyz || (!density && !own_density)))
+        return fail(h, FSR_ERR_INVALID_ARGUMENT, "null particle arrays");
     DeviceGuard g(h->device);
     cudaStream_t st = (cudaStream_t)stream;
     const uint64_t nn = std::max<uint64_t>(n, 1);
@@ -638,7 +646,7 @@ fsr_status fsr_reconstruct_host(fsr_handle* h, const fsr_frame_header* hdr, cons
     CK(h->in_den.ensure(4ull * nn));
     if (n) {
         CK(cudaMemcpyAsync(h->in_xyz.ptr, xyz, 12ull * n, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->in_den.ptr, density, 4ull * n, cudaMemcpyHostToDevice, st));
+        if (!own_density) CK(cudaMemcpyAsync(h->in_den.ptr, density, 4ull * n, cudaMemcpyHostToDevice, st));
     }
     h->frame_ready = false;
     fsr_status s = run_frame(h, *hdr, (const float*)h->in_xyz.ptr, (const float*)h->in_den.ptr, n, st);
@@ -741,6 +749,7 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
     case FSR_DBG_SMOOTHED: need = yu13 ? 12 * n : 0; break;
     case FSR_DBG_G: need = yu13 ? 36 * n : 0; break;
     case FSR_DBG_WELD_KEYS: need = (h->params.flags & FSR_FLAG_WELD) ? 8 * s.n_mesh_vertices : 0; break;
+    case FSR_DBG_DENSITY: need = 4 * n; break;
     default: return fail(h, FSR_ERR_INVALID_ARGUMENT, "unknown debug array %u", which);
     }
     if (bytes_needed) *bytes_needed = need;
@@ -782,6 +791,12 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
     }
     case FSR_DBG_VALID_CUBES: CK(cudaMemcpy(dst, h->valid.ptr, need, cudaMemcpyDeviceToHost)); break;
     case FSR_DBG_WELD_KEYS: CK(cudaMemcpy(dst, h->wkey.ptr, need, cudaMemcpyDeviceToHost)); break;
+    case FSR_DBG_DENSITY: {
+        std::vector<float> tmp(4 * n);
+        CK(cudaMemcpy(tmp.data(), h->sorted.ptr, 16 * n, cudaMemcpyDeviceToHost));
+        for (uint64_t i = 0; i < n; ++i) ((float*)dst)[i] = tmp[4 * i + 3];
+        break;
+    }
     case FSR_DBG_MEAN: CK(copy4(h->mean, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_SMOOTHED: CK(copy4(h->smoothed, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_G: {

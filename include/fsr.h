@@ -78,6 +78,14 @@ typedef struct fsr_params {
  * numbered in order of first use, with the position and normal of that first
  * copy.  The soup itself is unchanged. */
 #define FSR_FLAG_WELD 0x8u
+/* Compute each particle's density on the GPU instead of reading it (the
+ * density argument may be NULL): an SPH sum with the poly6 kernel over the
+ * particles within h, rho_i = m (315 / (64 pi h^3)) sum_j (1 - r_ij^2 / h^2)^3,
+ * the normalisation of the reference's field kernel (anisotropicW,
+ * ReconstructionCUDA.cuh:294-310).  The reference reads densities from the
+ * .xyz file and computes none.  fsr_backward is not available for such
+ * frames (the densities would depend on the positions). */
+#define FSR_FLAG_COMPUTE_DENSITY 0x10u
 
 /* The .xyz header (data_format.txt:1-15; ReconstructorGPU.cpp:215-251). */
 typedef struct fsr_frame_header {
@@ -197,8 +205,9 @@ typedef enum fsr_debug_array {
     FSR_DBG_MEAN = 9,            /* f32[N*3] Yu13 weighted means (sorted order) */
     FSR_DBG_SMOOTHED = 10,       /* f32[N*3] Yu13 smoothed positions */
     FSR_DBG_G = 11,              /* f32[N*9] Yu13 G matrices, row-major, sorted order (*) */
-    FSR_DBG_WELD_KEYS = 12       /* u64[3T] grid edge of each soup vertex, 3 x lower end point + axis
+    FSR_DBG_WELD_KEYS = 12,      /* u64[3T] grid edge of each soup vertex, 3 x lower end point + axis
                                     (with FSR_FLAG_WELD) */
+    FSR_DBG_DENSITY = 13         /* f32[N]  densities the frame used (sorted order) */
 } fsr_debug_array;
 
 fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes,

@@ -463,3 +463,25 @@ def cube_cases(kind: str, fr: Frame, cubes: np.ndarray) -> np.ndarray:
     lib.o_cases(_ptr(c), ctypes.c_uint32(c.size), _ptr(fr.phi), ctypes.byref(fr.scalar),
                 ctypes.byref(fr.simparam), _ptr(out))
     return out
+
+
+def sph_density(pos: np.ndarray, h: float, mass: float) -> np.ndarray:
+    """FP64 SPH density of every particle: m sigma / h^3 sum_j (1 - r_ij^2 /
+    h^2)^3 over the particles within h (i itself included), sigma = 315 /
+    (64 pi), the normalisation of the reference's field kernel (anisotropicW,
+    ReconstructionCUDA.cuh:294-310, at G = I / h).  The reference has no
+    density pass of its own (its .xyz files carry densities); this is the
+    checker of the library's FSR_FLAG_COMPUTE_DENSITY.  All pairs, in blocks
+    (for test-sized inputs)."""
+    p = np.asarray(pos, np.float64).reshape(-1, 3)
+    h = float(np.float32(h))
+    h2 = h * h
+    out = np.zeros(p.shape[0])
+    blk = 2048
+    for a in range(0, p.shape[0], blk):
+        d = p[a:a + blk, None, :] - p[None, :, :]
+        r2 = np.einsum("ijk,ijk->ij", d, d)
+        u = np.where(r2 < h2, 1.0 - r2 / h2, 0.0)
+        out[a:a + blk] = (u * u * u).sum(axis=1)
+    sigma = 315.0 / (64.0 * np.pi)
+    return float(np.float32(mass)) * sigma / h ** 3 * out
