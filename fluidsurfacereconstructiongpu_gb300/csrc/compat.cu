@@ -396,7 +396,7 @@ __global__ void k_cov_dense(uint64_t n, SimParam p, GridInfo spi, ParticleArray 
                         const float vx = __fsub_rn(o.x, m.x), vy = __fsub_rn(o.y, m.y), vz = __fsub_rn(o.z, m.z);
                         const float d = __fsqrt_rn(dot3_rn(vx, vy, vz));
                         if (d <= R) ++nn;
-                        if (d < R) acc.add(vx, vy, vz, d, R);
+                        if (d < R) acc.add(vx, vy, vz, __fdiv_rn(d, R));
                     }
                 }
         float G[9];

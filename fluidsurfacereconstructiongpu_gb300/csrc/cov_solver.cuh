@@ -105,9 +105,9 @@ __device__ __forceinline__ float make_G(const T V[3][3], const T w[3], float h_i
 // ReconstructionCUDA.cuh:282-292) for neighbours with d < R.
 struct CovAccum {
     Kahan c11, c22, c33, c12, c13, c23, wsum;
-    __device__ __forceinline__ void add(float vx, float vy, float vz, float d, float R)
+    // s = d / R, correctly rounded
+    __device__ __forceinline__ void add(float vx, float vy, float vz, float s)
     {
-        const float s = d / R;
         const float wt = 1.0f - s * s * s;
         wsum.add(wt);
         const float wx = wt * vx, wy = wt * vy;

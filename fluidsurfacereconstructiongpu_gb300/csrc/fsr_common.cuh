@@ -137,6 +137,24 @@ __device__ __forceinline__ Window narrow(const Window& w, float px, float py, fl
 // Margin applied to culling radii: relative 1e-4 plus 1e-4 of a cell.
 __device__ __forceinline__ float cull_radius(float r, float cs) { return r * 1.0001f + 1e-4f * cs; }
 
+// a / b correctly rounded (the same float as __fdiv_rn(a, b)) for a >= 0,
+// b > 0, given rb = RN(1 / b) computed once on the host.  Markstein's
+// theorem (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
+// Handbook of Floating-Point Arithmetic, "division with an FMA"): with y
+// within half an ulp of 1/b and q within one ulp of a/b, the remainder
+// r = a - b q is exact under an FMA and RN(q + r y) = RN(a / b), as long as
+// nothing underflows; tiny positive a (below 2^-64) take the IEEE division.
+// Three instructions instead of the IEEE division's sequence;
+// fsr_check_division verifies it against __fdiv_rn for every float a in
+// [0, 1.01 b].
+__device__ __forceinline__ float div_exact(float a, float b, float rb)
+{
+    if (a < 0x1p-64f && a > 0.0f) return __fdiv_rn(a, b);
+    const float q = __fmul_rn(a, rb);
+    const float r = fmaf(-q, b, a);
+    return fmaf(r, rb, q);
+}
+
 __device__ __forceinline__ bool band_has(const BandView& b, uint32_t v)
 {
     return (__ldg(b.bits + (v >> 5)) >> (v & 31u)) & 1u;

@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
 // reference's order with the reference's roundings.  smoothed.w = m / rho.
 __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
-                                                     float R_lt2, int coop_ok, float one_minus_lambda,
+                                                     float R_rcp, float R_lt2, int coop_ok, float one_minus_lambda,
                                                      float lambda, float mass, float4* __restrict__ mean,
                                                      float4* __restrict__ smoothed)
 {
@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
     auto add = [&](const float4& q) {
         const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
         if (!(d2 < R_lt2)) return;  // d >= R: weight 0, and +0 terms leave the sums unchanged
-        const float s = __fdiv_rn(__fsqrt_rn(d2), R);
+        const float s = div_exact(__fsqrt_rn(d2), R, R_rcp);
         const float wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
         ws = __fadd_rn(ws, wt);
         mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
@@ -549,7 +549,7 @@ __global__ void k_cov(CovArgs a, Counters* ctr)
         const float d2 = dot3_rn(vx, vy, vz);
         if (d2 < a.R_le2) {
             ++nn;
-            if (d2 < a.R_lt2) acc.add(vx, vy, vz, __fsqrt_rn(d2), a.R);
+            if (d2 < a.R_lt2) acc.add(vx, vy, vz, div_exact(__fsqrt_rn(d2), a.R, a.R_rcp));
         }
     };
     auto dist2 = [&](const float4& q) {
@@ -941,8 +941,8 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     // warps may walk the union of their windows when the cull radius stays
     // below two cells (see k_smooth)
     const int coop_ok = (R * 1.0001f + 1e-4f * sp.cs) < 2.0f * sp.cs * 0.9999f ? 1 : 0;
-    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, sqrt_threshold(R, false), coop_ok,
-                                                       oml, lambda, mass, mean, smoothed);
+    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, 1.0f / R, sqrt_threshold(R, false),
+                                                       coop_ok, oml, lambda, mass, mean, smoothed);
     ++g_launches;
 }
 
@@ -951,6 +951,7 @@ void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
     if (!a0.n) return;
     CovArgs a = a0;
     a.R_lt2 = sqrt_threshold(a.R, false);
+    a.R_rcp = 1.0f / a.R;
     a.R_le2 = sqrt_threshold(a.R, true);
     a.coop_ok = (a.R + a.R * 1.0001f + 1e-4f * a.sp.cs) < 2.0f * a.sp.cs * 0.9999f ? 1 : 0;
     k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);

@@ -87,6 +87,7 @@ struct CovArgs {
     float R, h, h2, h_inv, mass, sigma;
     uint32_t min_neighbors;
     float R_lt2, R_le2;  // squared-distance thresholds of d < R and d <= R (set by launch_cov)
+    float R_rcp;         // RN(1 / R), for div_exact (set by launch_cov)
     int coop_ok;         // compact warps may walk the union of their windows (set by launch_cov)
 };
 void launch_cov(const KernelCtx& c, const CovArgs& a, Counters* ctr);

@@ -1,0 +1,59 @@
+// Device self-checks of arithmetic shortcuts against CUDA's own operations.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "../../include/fsr.h"
+#include "fsr_common.cuh"
+
+namespace {
+
+// Every float a in [0, hi] (by bit pattern): div_exact(a, b, RN(1/b)) must
+// equal __fdiv_rn(a, b).
+__global__ void k_check_division(uint32_t hi_bits, float b, float rb, unsigned long long* bad,
+                                 unsigned long long* first_bad)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= hi_bits; i += stride) {
+        const float a = __uint_as_float((uint32_t)i);
+        const float x = fsr::div_exact(a, b, rb);
+        const float y = __fdiv_rn(a, b);
+        if (__float_as_uint(x) != __float_as_uint(y)) {
+            ++local;
+            atomicMin(first_bad, (unsigned long long)i);
+        }
+    }
+    if (local) atomicAdd(bad, local);
+}
+
+}  // namespace
+
+extern "C" fsr_status fsr_check_division(float b, uint64_t* n_checked, uint64_t* n_mismatch)
+{
+    if (!(b > 0.0f) || !std::isfinite(b) || !n_checked || !n_mismatch) return FSR_ERR_INVALID_ARGUMENT;
+    const float hi = b * 1.01f;
+    uint32_t hi_bits;
+    std::memcpy(&hi_bits, &hi, 4);
+    const float rb = 1.0f / b;
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return FSR_ERR_CUDA;
+    const unsigned long long init[2] = {0ull, ~0ull};
+    cudaError_t e = cudaMemcpy(d, init, 16, cudaMemcpyHostToDevice);
+    int sms = 1;
+    if (e == cudaSuccess) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_check_division<<<sms * 8, 256>>>(hi_bits, b, rb, d, d + 1);
+        e = cudaGetLastError();
+    }
+    unsigned long long out[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return FSR_ERR_CUDA;
+    *n_checked = (uint64_t)hi_bits + 1;
+    *n_mismatch = out[0];
+    return FSR_OK;
+}

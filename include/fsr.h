@@ -320,6 +320,12 @@ fsr_status fsr_batch_mesh_device(const fsr_batch* b, uint32_t frame, const float
 fsr_status fsr_batch_copy_mesh(const fsr_batch* b, uint32_t frame, float* pos, float* nrm, uint64_t capacity,
                                uint64_t* n_vertices);
 
+/* Self-check of the exact division the smoothing and covariance kernels use
+ * for d / R (an FMA refinement of d x RN(1/R), Markstein's theorem): runs it
+ * and __fdiv_rn on the current device for every float d in [0, 1.01 R] and
+ * counts the results that differ (0 expected). */
+fsr_status fsr_check_division(float R, uint64_t* n_checked, uint64_t* n_mismatch);
+
 /* ---- file formats -------------------------------------------------- */
 
 /* Parses an .xyz file (data_format.txt; ReconstructorGPU.cpp:200-290).
