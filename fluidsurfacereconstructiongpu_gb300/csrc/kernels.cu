@@ -524,7 +524,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
 // when the covariance's condition number exceeds 1e4.
 // Output record per particle: (x,y,z smoothed, r2max) (G row 0, coef)
 // (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
-__global__ void k_cov(CovArgs a, Counters* ctr)
+__global__ void __launch_bounds__(kThreads, 4) k_cov(CovArgs a, Counters* ctr)
 {
     __shared__ float4 s_q[kThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
