@@ -34,6 +34,7 @@ struct GroupArgs {
     Grid sp, sc;
     BandView band;
     const float4* grec;
+    const float4* qrec;  // per involved particle: (x~, r2max) (M00, 2M01, 2M02, coef) (M11, 2M12, M22, 0)
     const float4* smoothed;
     const uint2* ranges;
     const uint8_t* invol;
@@ -174,9 +175,11 @@ constexpr int kPassVerts = 32 * kPassTiles;
 
 // Per-warp shared memory of the forward kernel.
 struct WarpSlice {
-    float4 rec[32 * 4];          // the current chunk's candidate records, one per lane
+    float4 rec[32 * 3];          // the current chunk's candidate records, one per lane
     float4 vpos[kPassVerts];     // the pass's band vertices: position, band rank (bits)
     float4 box[2 * kPassTiles];  // per tile: lo, hi
+    float psum[kPassTiles][32];  // per tile and lane: sum over the involved candidates
+    float usum[kPassTiles][32];  // and over the non-involved ones
     uint32_t cstart[128];
     uint32_t cpre[kMaxCells + 1];
     uint32_t cinv[128];
@@ -267,15 +270,16 @@ __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ra
 // when v lies outside the support (q2 >= 1: the term is exactly zero).
 __device__ __forceinline__ bool term(const float4* r, float4 v, float& u3, float& coef)
 {
-    const float4 q0 = r[0], g0 = r[1], g1 = r[2], g2 = r[3];
-    const float rx = q0.x - v.x, ry = q0.y - v.y, rz = q0.z - v.z;
-    const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
-    const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
-    const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
-    const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+    // r[0] = (x~, r2max), r[1] = (M00, 2 M01, 2 M02, coef), r[2] = (M11, 2 M12, M22, 0)
+    // with M = G^T G, so q2 = |G d|^2 = d^T M d for d = x~ - v
+    const float4 q0 = r[0], m0 = r[1], m1 = r[2];
+    const float dx = q0.x - v.x, dy = q0.y - v.y, dz = q0.z - v.z;
+    const float t1 = fmaf(m0.x, dx, fmaf(m0.y, dy, m0.z * dz));
+    const float t2 = fmaf(m1.x, dy, m1.y * dz);
+    const float q2 = fmaf(dx, t1, fmaf(dy, t2, dz * (m1.z * dz)));
     const float u = 1.0f - q2;
     u3 = u * u * u;
-    coef = g0.w;
+    coef = m0.w;
     return q2 < 1.0f;
 }
 
@@ -352,9 +356,10 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             // thousands of them), added among themselves and joined at the
             // end, so that FP32 rounding does not drop or inflate them against
             // a sum of order 1
-            float sum[kPassTiles], sum_u[kPassTiles];
-#pragma unroll
-            for (int t = 0; t < kPassTiles; ++t) sum[t] = sum_u[t] = 0.f;
+            // the sums live in the warp's shared slice, so that the tile loops
+            // need not be unrolled (the kernel's code stays small enough for
+            // the instruction cache)
+            for (int t = 0; t < kPassTiles; ++t) w.psum[t][lane] = w.usum[t][lane] = 0.f;
             const uint32_t ncells = w.ncells, total_inv = w.total_inv;
             // involved candidates: staged with their G, culled per tile by
             // their support sphere, evaluated two at a time
@@ -365,28 +370,27 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 if (j < total_inv) {
                     int cell;
                     const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
-                    const float4* gsrc = a.grec + 4ull * i;
-                    r0 = __ldg(gsrc);
+                    const float4* qsrc = a.qrec + 3ull * i;
+                    r0 = __ldg(qsrc);
                     keep = reaches(r0, pl, ph);
                     if (keep) {
-                        float4* dst = w.rec + 4 * lane;
+                        float4* dst = w.rec + 3 * lane;
                         dst[0] = r0;
-                        dst[1] = __ldg(gsrc + 1);
-                        dst[2] = __ldg(gsrc + 2);
-                        dst[3] = __ldg(gsrc + 3);
+                        dst[1] = __ldg(qsrc + 1);
+                        dst[2] = __ldg(qsrc + 2);
                     }
                 }
                 const uint32_t any = __ballot_sync(0xffffffffu, keep);
                 __syncwarp();
                 if (any) {
-#pragma unroll
+#pragma unroll 1
                     for (int t = 0; t < kPassTiles; ++t) {
                         if ((uint32_t)t < ntiles) {
                             const uint32_t m = __ballot_sync(0xffffffffu, keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]));
                             const uint32_t v = 32 * t + lane;
                             if (m && v < nv) {
                                 const float4 vp = w.vpos[v];
-                                float s = sum[t];
+                                float s = w.psum[t][lane];
                                 // two kept candidates per step, evaluated without
                                 // branches; their terms enter the sum in order
                                 for (uint32_t mm = m; mm;) {
@@ -396,12 +400,12 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                                     const int kb = two ? __ffs(mm) - 1 : ka;
                                     mm &= two ? mm - 1u : ~0u;
                                     float ua, ub, ca, cb;
-                                    const bool ina = term(w.rec + 4 * ka, vp, ua, ca);
-                                    const bool inb = term(w.rec + 4 * kb, vp, ub, cb);
+                                    const bool ina = term(w.rec + 3 * ka, vp, ua, ca);
+                                    const bool inb = term(w.rec + 3 * kb, vp, ub, cb);
                                     if (ina) s = fmaf(ca, ua, s);
                                     if (two && inb) s = fmaf(cb, ub, s);
                                 }
-                                sum[t] = s;
+                                w.psum[t][lane] = s;
                             }
                         }
                     }
@@ -418,19 +422,19 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                     int cell;
                     const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
                     const float4 sm = __ldg(&a.smoothed[i]);
-                    w.rec[4 * lane] = make_float4(sm.x, sm.y, sm.z, a.sigma * sm.w);
+                    w.rec[lane] = make_float4(sm.x, sm.y, sm.z, a.sigma * sm.w);
                 }
                 const uint32_t cnt = min(32u, total - cb);
                 __syncwarp();
-#pragma unroll
+#pragma unroll 1
                 for (int t = 0; t < kPassTiles; ++t) {
                     const uint32_t v = 32 * t + lane;
                     if ((uint32_t)t < ntiles && v < nv) {
                         const float4 vp = w.vpos[v];
-                        float su = sum_u[t];
+                        float su = w.usum[t][lane];
                         uint32_t k = 0;
                         for (; k + 2 <= cnt; k += 2) {
-                            const float4 qa = w.rec[4 * k], qb = w.rec[4 * (k + 1)];
+                            const float4 qa = w.rec[k], qb = w.rec[k + 1];
                             const float ax = qa.x - vp.x, ay = qa.y - vp.y, az = qa.z - vp.z;
                             const float bx = qb.x - vp.x, by = qb.y - vp.y, bz = qb.z - vp.z;
                             const float q2a = fmaf(ax, ax, fmaf(ay, ay, az * az));
@@ -440,13 +444,13 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                             if (q2b < 1.0f) su = fmaf(qb.w, ub * ub * ub, su);
                         }
                         if (k < cnt) {
-                            const float4 qa = w.rec[4 * k];
+                            const float4 qa = w.rec[k];
                             const float ax = qa.x - vp.x, ay = qa.y - vp.y, az = qa.z - vp.z;
                             const float q2a = fmaf(ax, ax, fmaf(ay, ay, az * az));
                             const float ua = 1.0f - q2a;
                             if (q2a < 1.0f) su = fmaf(qa.w, ua * ua * ua, su);
                         }
-                        sum_u[t] = su;
+                        w.usum[t][lane] = su;
                     }
                 }
                 __syncwarp();
@@ -456,7 +460,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 const uint32_t v = 32 * t + lane;
                 if (v < nv) {
                     const uint32_t rank = __float_as_uint(w.vpos[v].w);
-                    if (rank < nb) a.phi[rank] = (sum[t] + sum_u[t]) - 0.5f;
+                    if (rank < nb) a.phi[rank] = (w.psum[t][lane] + w.usum[t][lane]) - 0.5f;
                 }
             }
             __syncwarp();
@@ -751,6 +755,7 @@ void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
     a.sc = f.sc;
     a.band = band;
     a.grec = f.grec;
+    a.qrec = f.qrec;
     a.smoothed = f.smoothed;
     a.ranges = f.ranges;
     a.invol = f.invol;

@@ -648,6 +648,17 @@ __global__ void __launch_bounds__(kThreads, 4) k_cov(CovArgs a, Counters* ctr)
     rec[1] = make_float4(G[0], G[1], G[2], a.sigma * det * sm.w);
     rec[2] = make_float4(G[3], G[4], G[5], 0.f);
     rec[3] = make_float4(G[6], G[7], G[8], 0.f);
+    // the field's form of the same kernel: q2 = |G d|^2 = d^T (G^T G) d
+    const float m00 = G[0] * G[0] + G[3] * G[3] + G[6] * G[6];
+    const float m11 = G[1] * G[1] + G[4] * G[4] + G[7] * G[7];
+    const float m22 = G[2] * G[2] + G[5] * G[5] + G[8] * G[8];
+    const float m01 = G[0] * G[1] + G[3] * G[4] + G[6] * G[7];
+    const float m02 = G[0] * G[2] + G[3] * G[5] + G[6] * G[8];
+    const float m12 = G[1] * G[2] + G[4] * G[5] + G[7] * G[8];
+    float4* q = a.qrec + 3ull * t;
+    q[0] = rec[0];
+    q[1] = make_float4(m00, 2.0f * m01, 2.0f * m02, rec[1].w);
+    q[2] = make_float4(m11, 2.0f * m12, m22, 0.f);
 }
 
 // ------------------------------------------------------------ marching cubes

@@ -81,6 +81,7 @@ struct CovArgs {
     const uint32_t* skeys;
     const uint8_t* invol;
     float4* grec;  // 4 float4 per particle: (x,y,z smoothed, r2max) (G rows, coef in row 0's w)
+    float4* qrec;  // 3 float4 per particle for the field: (x~, r2max) (M00, 2M01, 2M02, coef) (M11, 2M12, M22, 0), M = G^T G
     float4* crec;  // 2 float4 per particle: (C00 C01 C02 C11) (C12 C22 W, 1 if C was used else 0)
     float* cell_rmax;  // per cell: largest support radius + smoothing shift of its particles (zeroed per frame)
     uint32_t n;
@@ -96,6 +97,7 @@ struct AnisoFieldArgs {
     Grid sp, sc;
     const float4* smoothed;
     const float4* grec;
+    const float4* qrec;
     const uint2* ranges;
     const uint8_t* invol;
     const uint8_t* occ;

@@ -173,7 +173,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &qpos,   &valid,   &mean,   &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -233,6 +233,7 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         CK(h->mean.ensure(16ull * nn));
         CK(h->smoothed.ensure(16ull * nn));
         CK(h->grec.ensure(64ull * nn));
+        CK(h->qrec.ensure(48ull * nn));
         CK(h->covrec.ensure(32ull * nn));
     }
     if (p.method == FSR_METHOD_AKINCI12) CK(h->psurf.ensure(nn));
@@ -360,6 +361,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         ca.skeys = skeys;
         ca.invol = (const uint8_t*)h->invol.ptr;
         ca.grec = (float4*)h->grec.ptr;
+        ca.qrec = (float4*)h->qrec.ptr;
         ca.crec = (float4*)h->covrec.ptr;
         ca.cell_rmax = (float*)h->cell_rmax.ptr;
         ca.n = n;
@@ -377,6 +379,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.sc = sc;
         fa.smoothed = (const float4*)h->smoothed.ptr;
         fa.grec = (const float4*)h->grec.ptr;
+        fa.qrec = (const float4*)h->qrec.ptr;
         fa.ranges = ranges;
         fa.invol = (const uint8_t*)h->invol.ptr;
         fa.occ = occ;
