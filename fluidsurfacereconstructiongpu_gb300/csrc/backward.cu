@@ -638,6 +638,7 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
         fb.band = a.band;
         fb.smoothed = a.smoothed;
         fb.grec = a.grec;
+        fb.qrec = a.qrec;
         fb.ranges = a.ranges;
         fb.invol = a.invol;
         fb.cell_rmax = a.cell_rmax;

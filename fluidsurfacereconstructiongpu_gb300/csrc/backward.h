@@ -24,6 +24,7 @@ struct BwdArgs {
     const uint8_t* invol;
     const float4* smoothed;
     const float4* grec;
+    const float4* qrec;  // the field's records: (x~, r2max) (M00, 2M01, 2M02, coef) (M11, 2M12, M22, 0)
     const uint2* ranges;
     const float* cell_rmax;  // Yu13: per cell, largest support reach of its particles
     const float4* mv;        // ZB05: per band vertex (mean - v, weight sum)

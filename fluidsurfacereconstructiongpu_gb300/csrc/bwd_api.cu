@@ -105,6 +105,7 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     a.invol = (const uint8_t*)h->invol.ptr;
     a.smoothed = (const float4*)h->smoothed.ptr;
     a.grec = (const float4*)h->grec.ptr;
+    a.qrec = (const float4*)h->qrec.ptr;
     a.ranges = (const uint2*)h->ranges.ptr;
     a.cell_rmax = (const float*)h->cell_rmax.ptr;
     a.mv = (const float4*)h->mv.ptr;

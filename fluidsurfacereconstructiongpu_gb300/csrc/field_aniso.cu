@@ -533,6 +533,7 @@ struct BwdGroupArgs {
     Grid sp, sc;
     BandView band;
     const float4* grec;
+    const float4* qrec;
     const float4* smoothed;
     const uint2* ranges;
     const uint8_t* invol;
@@ -653,7 +654,6 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
             if (!(box_dist2(r0.x, r0.y, r0.z, glo, ghi) < r0.w)) continue;
             const float coef = g0.w;
             float gxs = 0.f, gys = 0.f, gzs = 0.f, sc = 0.f;
-            float gg[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (!inv) {
                 // unscaled kernel (G = I, support 1): d/dx~ (1 - |r|^2)^3 = -6 (1 - |r|^2)^2 r;
                 // no dL/dG.  Candidates come cell by cell, so a warp's threads
@@ -672,6 +672,13 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
                 if (gxs != 0.f || gys != 0.f || gzs != 0.f) atomicAdd(a.gsmooth + i, make_float4(gxs, gys, gzs, 0.f));
                 continue;
             }
+            // per pair, with M = G^T G (the forward's quadratic form) and
+            // B = -3 g c (1 - q2)^2:  dL/dx~ += 2 B M d,  dL/dM += B d d^T
+            // (S, symmetric); dL/dG = 2 G S once per candidate at the end
+            const float4 qa = __ldg(a.qrec + 3ull * i + 1), qb = __ldg(a.qrec + 3ull * i + 2);
+            const float m00 = qa.x, m01 = 0.5f * qa.y, m02 = 0.5f * qa.z;
+            const float m11 = qb.x, m12 = 0.5f * qb.y, m22 = qb.z;
+            float s00 = 0.f, s01 = 0.f, s02 = 0.f, s11 = 0.f, s12 = 0.f, s22 = 0.f;
             for (uint32_t k = 0; k < nch; ++k) {
                 if (!(box_dist2(r0.x, r0.y, r0.z, cbox[2 * k], cbox[2 * k + 1]) < r0.w)) continue;
                 const uint32_t qe = min(nv, 32 * k + 32);
@@ -680,29 +687,38 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
                     const float rx = r0.x - v.x, ry = r0.y - v.y, rz = r0.z - v.z;
                     const float d2 = fmaf(rx, rx, fmaf(ry, ry, rz * rz));
                     if (!(d2 < r0.w)) continue;
-                    const float tx = fmaf(g0.x, rx, fmaf(g0.y, ry, g0.z * rz));
-                    const float ty = fmaf(g1.x, rx, fmaf(g1.y, ry, g1.z * rz));
-                    const float tz = fmaf(g2.x, rx, fmaf(g2.y, ry, g2.z * rz));
-                    const float q2 = fmaf(tx, tx, fmaf(ty, ty, tz * tz));
+                    const float a0 = fmaf(m00, rx, fmaf(m01, ry, m02 * rz));
+                    const float a1 = fmaf(m01, rx, fmaf(m11, ry, m12 * rz));
+                    const float a2 = fmaf(m02, rx, fmaf(m12, ry, m22 * rz));
+                    const float q2 = fmaf(rx, a0, fmaf(ry, a1, rz * a2));
                     if (!(q2 < 1.0f)) continue;
                     const float u = 1.0f - q2;
-                    const float A = -6.0f * v.w * coef * u * u;
-                    gxs += A * (g0.x * tx + g1.x * ty + g2.x * tz);
-                    gys += A * (g0.y * tx + g1.y * ty + g2.y * tz);
-                    gzs += A * (g0.z * tx + g1.z * ty + g2.z * tz);
-                    gg[0] += A * tx * rx; gg[1] += A * tx * ry; gg[2] += A * tx * rz;
-                    gg[3] += A * ty * rx; gg[4] += A * ty * ry; gg[5] += A * ty * rz;
-                    gg[6] += A * tz * rx; gg[7] += A * tz * ry; gg[8] += A * tz * rz;
-                    sc += v.w * u * u * u;
+                    const float B = -3.0f * v.w * coef * u * u;
+                    const float B2 = B + B;
+                    gxs = fmaf(B2, a0, gxs);
+                    gys = fmaf(B2, a1, gys);
+                    gzs = fmaf(B2, a2, gzs);
+                    const float bx = B * rx, by = B * ry, bz = B * rz;
+                    s00 = fmaf(bx, rx, s00);
+                    s01 = fmaf(bx, ry, s01);
+                    s02 = fmaf(bx, rz, s02);
+                    s11 = fmaf(by, ry, s11);
+                    s12 = fmaf(by, rz, s12);
+                    s22 = fmaf(bz, rz, s22);
+                    sc = fmaf(v.w, u * u * u, sc);
                 }
             }
             if (gxs != 0.f || gys != 0.f || gzs != 0.f || sc != 0.f) {
                 atomicAdd(a.gsmooth + i, make_float4(gxs, gys, gzs, sc));
-                if (inv) {
-                    atomicAdd(a.gG + 3ull * i, make_float4(gg[0], gg[1], gg[2], 0.f));
-                    atomicAdd(a.gG + 3ull * i + 1, make_float4(gg[3], gg[4], gg[5], 0.f));
-                    atomicAdd(a.gG + 3ull * i + 2, make_float4(gg[6], gg[7], gg[8], 0.f));
-                }
+                // dL/dG = 2 G S
+                auto row = [&](float4 g) {
+                    return make_float4(2.0f * (g.x * s00 + g.y * s01 + g.z * s02),
+                                       2.0f * (g.x * s01 + g.y * s11 + g.z * s12),
+                                       2.0f * (g.x * s02 + g.y * s12 + g.z * s22), 0.f);
+                };
+                atomicAdd(a.gG + 3ull * i, row(g0));
+                atomicAdd(a.gG + 3ull * i + 1, row(g1));
+                atomicAdd(a.gG + 3ull * i + 2, row(g2));
             }
         }
         __syncthreads();
@@ -728,6 +744,7 @@ bool launch_field_aniso_backward_grouped(const KernelCtx& c, const AnisoBwdArgs&
     a.sc = f.sc;
     a.band = f.band;
     a.grec = f.grec;
+    a.qrec = f.qrec;
     a.smoothed = f.smoothed;
     a.ranges = f.ranges;
     a.invol = f.invol;

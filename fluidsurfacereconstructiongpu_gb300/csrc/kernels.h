@@ -120,6 +120,7 @@ struct AnisoBwdArgs {
     BandView band;
     const float4* smoothed;
     const float4* grec;
+    const float4* qrec;
     const uint2* ranges;
     const uint8_t* invol;
     const float* cell_rmax;
