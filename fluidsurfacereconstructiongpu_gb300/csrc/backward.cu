@@ -530,7 +530,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
         for (int i = 0; i < 3; ++i)
             for (int k = 0; k < 3; ++k) gA[i][k] = gC[i][k] * iw;
     }
-    const float R = f.R, invR3 = 1.0f / (R * R * R);
+    const float R = f.R, invR = 1.0f / R, invR3 = invR * invR * invR;
     float gmx = 0.f, gmy = 0.f, gmz = 0.f;
     walk_windows(w, act, f.coop_ok != 0, f.sp, f.ranges, f.sorted, s_q + (threadIdx.x & ~31u),
                  [&](uint32_t i, const float4& q) {
@@ -538,7 +538,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
         const float d2 = dot3_rn(vx, vy, vz);
         if (!(d2 < f.R_lt2)) return;  // the forward's weight test (d < R), exactly
         const float d = __fsqrt_rn(d2);
-        const float s = d / R;
+        const float s = d * invR;
         const float wt = 1.0f - s * s * s;
         const float Avx = gA[0][0] * vx + gA[0][1] * vy + gA[0][2] * vz;
         const float Avy = gA[1][0] * vx + gA[1][1] * vy + gA[1][2] * vz;
@@ -579,6 +579,7 @@ __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4*
                                 p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
         const float iw = 1.0f / m.w;
         const float gnx = gmx * iw, gny = gmy * iw, gnz = gmz * iw;
+        const float invR = 1.0f / R, invR3 = invR * invR * invR;
         walk_windows(w, act, coop_ok != 0, sp, ranges, sorted, s_q + (threadIdx.x & ~31u),
                      [&](uint32_t i, const float4& q) {
             // the forward's neighbour decision, exactly
@@ -586,17 +587,13 @@ __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4*
             if (!(d2 < R_lt2)) return;
             const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
             const float d = sqrtf(d2);
-            const float s = d / R;
+            const float s = d * invR;
             const float wt = 1.0f - s * s * s;
             // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
             const float gw = gnx * (q.x - m.x) + gny * (q.y - m.y) + gnz * (q.z - m.z);
-            float ex = 0.f, ey = 0.f, ez = 0.f;
-            if (d > 0.f) {
-                const float k = gw * (-3.0f * s * s / R) / d;  // dw/dd * (x_i - x_j)/d
-                ex = k * dx;
-                ey = k * dy;
-                ez = k * dz;
-            }
+            // dw/dd (x_i - x_j) / d = -3 d / R^3 (x_i - x_j)
+            const float k = gw * (-3.0f * d * invR3);
+            const float ex = k * dx, ey = k * dy, ez = k * dz;
             gix += ex;
             giy += ey;
             giz += ez;
