@@ -537,7 +537,7 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
         const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
         const float d2 = dot3_rn(vx, vy, vz);
         if (!(d2 < f.R_lt2)) return;  // the forward's weight test (d < R), exactly
-        const float d = __fsqrt_rn(d2);
+        const float d = d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;  // the gradient needs no correctly rounded root
         const float s = d * invR;
         const float wt = 1.0f - s * s * s;
         const float Avx = gA[0][0] * vx + gA[0][1] * vy + gA[0][2] * vz;
@@ -586,7 +586,7 @@ __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4*
             const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
             if (!(d2 < R_lt2)) return;
             const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-            const float d = sqrtf(d2);
+            const float d = d2 > 0.f ? d2 * rsqrtf(d2) : 0.f;
             const float s = d * invR;
             const float wt = 1.0f - s * s * s;
             // mean = sum w x / W: dL/dx_j += w gN, dL/dw = <gN, x_j - mean>
