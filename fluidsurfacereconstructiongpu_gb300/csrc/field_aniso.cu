@@ -172,6 +172,7 @@ constexpr int kFT = 128;                 // threads per block of the forward ker
 constexpr int kFWarps = kFT / 32;
 constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept in registers)
 constexpr int kPassVerts = 32 * kPassTiles;
+constexpr int kMoments = 35;             // moments of the unscaled kernel's polynomial (unscaled_sum)
 
 // Per-warp shared memory of the forward kernel.
 struct WarpSlice {
@@ -181,6 +182,8 @@ struct WarpSlice {
     float psum[kPassTiles][32];  // per tile and lane: sum over the involved candidates
     float usum[kPassTiles][32];  // and over the non-involved ones
     uint16_t order[kPassVerts];  // the pass's vertices in brick order (tile t: entries 32t .. 32t+31)
+    float mom[kMoments];         // moments of the group's non-involved candidates (unscaled_moments)
+    uint32_t use_mom;            // the moment form applies to this group
     uint32_t cstart[128];
     uint32_t cpre[kMaxCells + 1];
     uint32_t cinv[128];
@@ -292,6 +295,76 @@ __device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
 }
 
+// The unscaled kernel's part of the field at vertex v, sum_j c_j (1 - |x_j -
+// v|^2)^3 over the group's non-involved candidates j, is one polynomial in
+// v for the whole group when every candidate is inside the support of every
+// vertex (then no term is cut at q2 = 1).  With y_j = x_j - o, z = v - o
+// (o: the centre of the group's vertex box), a_j = 1 - |y_j|^2, w = |z|^2:
+//   1 - |x_j - v|^2 = (a_j - w) + 2 y_j.z, and the cube of that sums to
+//   sum c (a-w)^3 + 6 sum c (a-w)^2 (y.z) + 12 sum c (a-w) (y.z)^2 + 8 sum c (y.z)^3,
+// which needs 35 moments of (c, a, y): A_k = sum c a^k (k = 0..3),
+// B_k = sum c a^k y (k = 0..2), C_k = sum c a^k y y^T (k = 0, 1) and
+// D = sum c y y y.  The expansion holds exactly; it is used when
+// max |y| + max |z| < 0.5 (all pairs well inside the unit support, every
+// term of order 1, no cancellation), else the candidates are streamed.
+
+struct MomAcc {
+    float m[kMoments];
+    __device__ __forceinline__ void zero()
+    {
+#pragma unroll
+        for (int k = 0; k < kMoments; ++k) m[k] = 0.f;
+    }
+    __device__ __forceinline__ void add(float c, float yx, float yy, float yz)
+    {
+        const float a = 1.0f - fmaf(yx, yx, fmaf(yy, yy, yz * yz));
+        const float ca = c * a, ca2 = ca * a;
+        m[0] += c;
+        m[1] += ca;
+        m[2] += ca2;
+        m[3] += ca2 * a;
+        m[4] = fmaf(c, yx, m[4]);   m[5] = fmaf(c, yy, m[5]);   m[6] = fmaf(c, yz, m[6]);
+        m[7] = fmaf(ca, yx, m[7]);  m[8] = fmaf(ca, yy, m[8]);  m[9] = fmaf(ca, yz, m[9]);
+        m[10] = fmaf(ca2, yx, m[10]); m[11] = fmaf(ca2, yy, m[11]); m[12] = fmaf(ca2, yz, m[12]);
+        const float cx = c * yx, cy = c * yy, cz = c * yz;
+        m[13] = fmaf(cx, yx, m[13]); m[14] = fmaf(cy, yy, m[14]); m[15] = fmaf(cz, yz, m[15]);
+        m[16] = fmaf(cx, yy, m[16]); m[17] = fmaf(cx, yz, m[17]); m[18] = fmaf(cy, yz, m[18]);
+        m[19] = fmaf(cx * a, yx, m[19]); m[20] = fmaf(cy * a, yy, m[20]); m[21] = fmaf(cz * a, yz, m[21]);
+        m[22] = fmaf(cx * a, yy, m[22]); m[23] = fmaf(cx * a, yz, m[23]); m[24] = fmaf(cy * a, yz, m[24]);
+        const float cxx = cx * yx, cyy = cy * yy, czz = cz * yz;
+        m[25] = fmaf(cxx, yx, m[25]);  // xxx
+        m[26] = fmaf(cyy, yy, m[26]);  // yyy
+        m[27] = fmaf(czz, yz, m[27]);  // zzz
+        m[28] = fmaf(cxx, yy, m[28]);  // xxy
+        m[29] = fmaf(cxx, yz, m[29]);  // xxz
+        m[30] = fmaf(cyy, yx, m[30]);  // xyy
+        m[31] = fmaf(cyy, yz, m[31]);  // yyz
+        m[32] = fmaf(czz, yx, m[32]);  // xzz
+        m[33] = fmaf(czz, yy, m[33]);  // yzz
+        m[34] = fmaf(cx * yy, yz, m[34]);  // xyz
+    }
+};
+
+// The polynomial at z = v - o.
+__device__ __forceinline__ float unscaled_sum(const float* m, float zx, float zy, float zz)
+{
+    const float w = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+    const float t1 = fmaf(w, fmaf(w, fmaf(-w, m[0], 3.0f * m[1]), -3.0f * m[2]), m[3]);
+    const float b0 = fmaf(m[4], zx, fmaf(m[5], zy, m[6] * zz));
+    const float b1 = fmaf(m[7], zx, fmaf(m[8], zy, m[9] * zz));
+    const float b2 = fmaf(m[10], zx, fmaf(m[11], zy, m[12] * zz));
+    const float t2 = 6.0f * fmaf(w, fmaf(w, b0, -2.0f * b1), b2);
+    const float xx = zx * zx, yy = zy * zy, zz2 = zz * zz, xy = zx * zy, xz = zx * zz, yz = zy * zz;
+    const float q0 = fmaf(m[13], xx, fmaf(m[14], yy, fmaf(m[15], zz2, 2.0f * fmaf(m[16], xy, fmaf(m[17], xz, m[18] * yz)))));
+    const float q1 = fmaf(m[19], xx, fmaf(m[20], yy, fmaf(m[21], zz2, 2.0f * fmaf(m[22], xy, fmaf(m[23], xz, m[24] * yz)))));
+    const float t3 = 12.0f * fmaf(-w, q0, q1);
+    const float d3 = fmaf(m[25], xx * zx, fmaf(m[26], yy * zy, m[27] * zz2 * zz));
+    const float d21 = fmaf(m[28], xx * zy, fmaf(m[29], xx * zz, fmaf(m[30], yy * zx,
+                      fmaf(m[31], yy * zz, fmaf(m[32], zz2 * zx, m[33] * zz2 * zy)))));
+    const float t4 = 8.0f * fmaf(6.0f, m[34] * xy * zz, fmaf(3.0f, d21, d3));
+    return (t1 + t2) + (t3 + t4);
+}
+
 // One warp per window group, groups handed out dynamically; no block-wide
 // barriers.  The warp walks the group's index box 32 vertices at a time and
 // collects up to 256 band vertices per pass (8 tiles of 32).  Per pass it
@@ -329,6 +402,32 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                                      vpos1(hi[2] - 1, a.sc.min[2], a.sc.cs)};
                 total = warp_candidates(a.sp, a.ranges, a.invol, a.reach, c, b0, b1, w);
                 tables = true;
+                // moments of the non-involved candidates about the box centre
+                const float ox = 0.5f * (b0[0] + b1[0]), oy = 0.5f * (b0[1] + b1[1]), oz = 0.5f * (b0[2] + b1[2]);
+                const float hx = 0.5f * (b1[0] - b0[0]), hy = 0.5f * (b1[1] - b0[1]), hz = 0.5f * (b1[2] - b0[2]);
+                MomAcc acc;
+                acc.zero();
+                float y2max = 0.f;
+                for (uint32_t j = w.total_inv + lane; j < total; j += 32) {
+                    int cell;
+                    const uint32_t i = candidate(j, tabs, &cell, (int)w.ncells);
+                    const float4 sm = __ldg(&a.smoothed[i]);
+                    const float yx = sm.x - ox, yy = sm.y - oy, yz = sm.z - oz;
+                    y2max = fmaxf(y2max, fmaf(yx, yx, fmaf(yy, yy, yz * yz)));
+                    acc.add(a.sigma * sm.w, yx, yy, yz);
+                }
+#pragma unroll
+                for (int k = 0; k < kMoments; ++k) {
+                    float v = acc.m[k];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0) w.mom[k] = v;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) y2max = fmaxf(y2max, __shfl_xor_sync(0xffffffffu, y2max, o));
+                const float zmax = sqrtf(fmaf(hx, hx, fmaf(hy, hy, hz * hz)));
+                if (lane == 0) w.use_mom = (sqrtf(y2max) + zmax) * 1.001f < 0.5f ? 1u : 0u;
+                __syncwarp();
             }
             const uint32_t ntiles = (nv + 31) / 32;
             // the pass's box
@@ -481,10 +580,25 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 __syncwarp();
             }
             // non-involved candidates: G = I and support 1 (world units), which
-            // reaches every vertex of the window, so no culling; only the
-            // position and the coefficient sigma m / rho are staged, and q2 is
-            // |x~ - v|^2 (what the general path gives for G = I, bit for bit)
-            for (uint32_t cb = total_inv; cb < total; cb += 32) {
+            // reaches every vertex of the window.  Their sum is the group's
+            // moment polynomial when it applies; else they are streamed: only
+            // the position and the coefficient sigma m / rho are staged, and
+            // q2 is |x~ - v|^2
+            const bool use_mom = w.use_mom != 0u;
+            if (use_mom) {
+                const float ox = 0.5f * (vpos1(lo[0], a.sc.min[0], a.sc.cs) + vpos1(hi[0] - 1, a.sc.min[0], a.sc.cs));
+                const float oy = 0.5f * (vpos1(lo[1], a.sc.min[1], a.sc.cs) + vpos1(hi[1] - 1, a.sc.min[1], a.sc.cs));
+                const float oz = 0.5f * (vpos1(lo[2], a.sc.min[2], a.sc.cs) + vpos1(hi[2] - 1, a.sc.min[2], a.sc.cs));
+#pragma unroll 1
+                for (int t = 0; t < kPassTiles; ++t) {
+                    const uint32_t v = 32 * t + lane;
+                    if ((uint32_t)t < ntiles && v < nv) {
+                        const float4 vp = w.vpos[w.order[v]];
+                        w.usum[t][lane] = unscaled_sum(w.mom, vp.x - ox, vp.y - oy, vp.z - oz);
+                    }
+                }
+            }
+            for (uint32_t cb = use_mom ? total : total_inv; cb < total; cb += 32) {
                 const uint32_t j = cb + lane;
                 if (j < total) {
                     int cell;
