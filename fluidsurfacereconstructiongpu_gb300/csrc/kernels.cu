@@ -423,6 +423,50 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
     }
 }
 
+// Box of the warp's active centres grown by r: a candidate outside it lies
+// beyond r of every active lane's centre.
+struct WarpBox {
+    float lo[3], hi[3];
+    __device__ __forceinline__ bool holds(const float4& q) const
+    {
+        return q.x >= lo[0] && q.x <= hi[0] && q.y >= lo[1] && q.y <= hi[1] && q.z >= lo[2] && q.z <= hi[2];
+    }
+};
+
+__device__ __forceinline__ WarpBox warp_box(bool active, float x, float y, float z, float r)
+{
+    WarpBox b;
+    float lo[3] = {active ? x : 3.0e38f, active ? y : 3.0e38f, active ? z : 3.0e38f};
+    float hi[3] = {active ? x : -3.0e38f, active ? y : -3.0e38f, active ? z : -3.0e38f};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        b.lo[a] = lo[a] - r;
+        b.hi[a] = hi[a] + r;
+    }
+    return b;
+}
+
+// Stages the warp's next chunk of candidates [base, end): the ones inside
+// the box go to sq in their order; returns how many.
+__device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src, uint32_t base, uint32_t end,
+                                                 const WarpBox& box, float4* sq, int lane)
+{
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool keep = false;
+    if (base + lane < end) {
+        q = __ldg(&src[base + lane]);
+        keep = box.holds(q);
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+    if (keep) sq[__popc(m & ((1u << lane) - 1u))] = q;
+    return __popc(m);
+}
+
 // ------------------------------------------------------------ anisotropic path
 // calculationOfMeanAndSmoothParticles (cu:598-658).  The mean decides the
 // neighbour counts of the covariance stage, so it is summed in the
@@ -484,14 +528,16 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
         compact = compact && uhi[a] - ulo[a] <= 3;
     }
     if (compact) {
+        // candidates beyond R of every lane's particle are dropped at staging
+        // (their weights are 0: the sums are unchanged)
+        const WarpBox box = warp_box(active, p.x, p.y, p.z, cull_radius(R, sp.cs));
         for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
             for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(ulo[0], uhi[0], yy, zz, beg, end);
                 for (uint32_t base = beg; base < end; base += 32) {
-                    if (base + lane < end) sq[lane] = __ldg(&sorted[base + lane]);
+                    const uint32_t cnt = stage_in_box(sorted, base, end, box, sq, lane);
                     __syncwarp();
-                    const uint32_t cnt = min(32u, end - base);
                     for (uint32_t k = 0; k < cnt; ++k) add(sq[k]);
                     __syncwarp();
                 }
@@ -581,14 +627,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_cov(CovArgs a, Counters* ctr)
         compact = compact && uhi[ax] - ulo[ax] <= 3;
     }
     if (compact) {
+        // candidates beyond R of every lane's mean are dropped at staging
+        const WarpBox box = warp_box(act, m.x, m.y, m.z, cull_radius(a.R, a.sp.cs));
         for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
             for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(ulo[0], uhi[0], yy, zz, beg, end);
                 for (uint32_t base = beg; base < end; base += 32) {
-                    if (base + lane < end) sq[lane] = __ldg(&a.sorted[base + lane]);
+                    const uint32_t cnt = stage_in_box(a.sorted, base, end, box, sq, lane);
                     __syncwarp();
-                    const uint32_t cnt = min(32u, end - base);
                     uint32_t k = 0;
                     for (; k + 4 <= cnt; k += 4) {
                         const float4 q0 = sq[k], q1 = sq[k + 1], q2 = sq[k + 2], q3 = sq[k + 3];
