@@ -415,10 +415,13 @@ __device__ void g_to_c(const T V[3][3], const T l[3], float h_inv, const float g
 // sq at a time (one load per particle for the whole warp); the caller sets
 // coop only when every particle the union adds fails each lane's own range
 // test, so each lane still sees exactly the particles that matter to it.
+// Staged particles outside the box of the active lanes' centres (cx, cy, cz)
+// grown by r are dropped (they fail every lane's range test); the others
+// keep their order, their index rides in the staged w.
 template <class Fn>
 __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool coop, const Grid& sp,
                                              const uint2* __restrict__ ranges, const float4* __restrict__ sorted,
-                                             float4* sq, Fn fn)
+                                             float4* sq, float cx, float cy, float cz, float r, Fn fn)
 {
     const int lane = threadIdx.x & 31;
     auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
@@ -442,16 +445,27 @@ __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool 
         compact = compact && uhi[a] - ulo[a] <= 3;
     }
     if (compact) {
+        const WarpBox box = warp_box(active, cx, cy, cz, r);
         for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
             for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(ulo[0], uhi[0], yy, zz, beg, end);
                 for (uint32_t b = beg; b < end; b += 32) {
-                    if (b + lane < end) sq[lane] = __ldg(&sorted[b + lane]);
+                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                    bool keep = false;
+                    if (b + lane < end) {
+                        q = __ldg(&sorted[b + lane]);
+                        keep = box.holds(q);
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+                    if (keep) sq[__popc(m & ((1u << lane) - 1u))] = make_float4(q.x, q.y, q.z, __uint_as_float(b + lane));
                     __syncwarp();
-                    const uint32_t cnt = min(32u, end - b);
+                    const uint32_t cnt = __popc(m);
                     if (active)
-                        for (uint32_t k = 0; k < cnt; ++k) fn(b + k, sq[k]);
+                        for (uint32_t k = 0; k < cnt; ++k) {
+                            const float4 e = sq[k];
+                            fn(__float_as_uint(e.w), e);
+                        }
                     __syncwarp();
                 }
             }
@@ -532,8 +546,8 @@ __global__ void k_cov_backward(BwdArgs a, CovArgs f)
     }
     const float R = f.R, invR = 1.0f / R, invR3 = invR * invR * invR;
     float gmx = 0.f, gmy = 0.f, gmz = 0.f;
-    walk_windows(w, act, f.coop_ok != 0, f.sp, f.ranges, f.sorted, s_q + (threadIdx.x & ~31u),
-                 [&](uint32_t i, const float4& q) {
+    walk_windows(w, act, f.coop_ok != 0, f.sp, f.ranges, f.sorted, s_q + (threadIdx.x & ~31u), m.x, m.y, m.z,
+                 cull_radius(R, f.sp.cs), [&](uint32_t i, const float4& q) {
         const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
         const float d2 = dot3_rn(vx, vy, vz);
         if (!(d2 < f.R_lt2)) return;  // the forward's weight test (d < R), exactly
@@ -580,7 +594,8 @@ __global__ void k_smooth_backward(BwdArgs a, const float4* sorted, const float4*
         const float iw = 1.0f / m.w;
         const float gnx = gmx * iw, gny = gmy * iw, gnz = gmz * iw;
         const float invR = 1.0f / R, invR3 = invR * invR * invR;
-        walk_windows(w, act, coop_ok != 0, sp, ranges, sorted, s_q + (threadIdx.x & ~31u),
+        walk_windows(w, act, coop_ok != 0, sp, ranges, sorted, s_q + (threadIdx.x & ~31u), p.x, p.y, p.z,
+                     cull_radius(R, sp.cs),
                      [&](uint32_t i, const float4& q) {
             // the forward's neighbour decision, exactly
             const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));

@@ -137,6 +137,34 @@ __device__ __forceinline__ Window narrow(const Window& w, float px, float py, fl
 // Margin applied to culling radii: relative 1e-4 plus 1e-4 of a cell.
 __device__ __forceinline__ float cull_radius(float r, float cs) { return r * 1.0001f + 1e-4f * cs; }
 
+// Box of the warp's active centres grown by r: a candidate outside it lies
+// beyond r of every active lane's centre.
+struct WarpBox {
+    float lo[3], hi[3];
+    __device__ __forceinline__ bool holds(const float4& q) const
+    {
+        return q.x >= lo[0] && q.x <= hi[0] && q.y >= lo[1] && q.y <= hi[1] && q.z >= lo[2] && q.z <= hi[2];
+    }
+};
+
+__device__ __forceinline__ WarpBox warp_box(bool active, float x, float y, float z, float r)
+{
+    WarpBox b;
+    float lo[3] = {active ? x : 3.0e38f, active ? y : 3.0e38f, active ? z : 3.0e38f};
+    float hi[3] = {active ? x : -3.0e38f, active ? y : -3.0e38f, active ? z : -3.0e38f};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+        b.lo[a] = lo[a] - r;
+        b.hi[a] = hi[a] + r;
+    }
+    return b;
+}
+
 // a / b correctly rounded (the same float as __fdiv_rn(a, b)) for a >= 0,
 // b > 0, given rb = RN(1 / b) computed once on the host.  Markstein's
 // theorem (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,

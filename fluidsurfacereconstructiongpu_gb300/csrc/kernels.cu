@@ -379,6 +379,8 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
             compact = compact && uhi[ax3] - ulo[ax3] <= 3;
         }
         if (compact) {
+            // particles beyond h of every lane's vertex are dropped at staging
+            const WarpBox box = warp_box(active, vx, vy, vz, cull_radius(a.h, a.sp.cs));
             for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
                 for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
                     const bool row_in = active && zz >= w.lo[2] && zz <= w.hi[2] && yy >= w.lo[1] && yy <= w.hi[1];
@@ -386,12 +388,20 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
                     uint32_t beg, end;
                     row_range(ulo[0], uhi[0], yy, zz, beg, end);
                     for (uint32_t b = beg; b < end; b += 32) {
+                        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                        bool keep = false;
                         if (b + lane < end) {
-                            sq[lane] = __ldg(&a.sorted[b + lane]);
-                            sc[lane] = __ldg(&a.skeys[b + lane]) % a.sp.res[0];
+                            q = __ldg(&a.sorted[b + lane]);
+                            keep = box.holds(q);
+                        }
+                        const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+                        if (keep) {
+                            const uint32_t slot = __popc(mk & ((1u << lane) - 1u));
+                            sq[slot] = q;
+                            sc[slot] = __ldg(&a.skeys[b + lane]) % a.sp.res[0];
                         }
                         __syncwarp();
-                        const uint32_t cnt = min(32u, end - b);
+                        const uint32_t cnt = __popc(mk);
                         if (row_in)
                             for (uint32_t k = 0; k < cnt; ++k) {
                                 const int cx = (int)sc[k];
@@ -421,34 +431,6 @@ __global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Co
         }
         a.phi[t] = phi;
     }
-}
-
-// Box of the warp's active centres grown by r: a candidate outside it lies
-// beyond r of every active lane's centre.
-struct WarpBox {
-    float lo[3], hi[3];
-    __device__ __forceinline__ bool holds(const float4& q) const
-    {
-        return q.x >= lo[0] && q.x <= hi[0] && q.y >= lo[1] && q.y <= hi[1] && q.z >= lo[2] && q.z <= hi[2];
-    }
-};
-
-__device__ __forceinline__ WarpBox warp_box(bool active, float x, float y, float z, float r)
-{
-    WarpBox b;
-    float lo[3] = {active ? x : 3.0e38f, active ? y : 3.0e38f, active ? z : 3.0e38f};
-    float hi[3] = {active ? x : -3.0e38f, active ? y : -3.0e38f, active ? z : -3.0e38f};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
-            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
-        }
-        b.lo[a] = lo[a] - r;
-        b.hi[a] = hi[a] + r;
-    }
-    return b;
 }
 
 // Stages the warp's next chunk of candidates [base, end): the ones inside
