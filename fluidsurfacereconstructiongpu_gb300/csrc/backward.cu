@@ -672,11 +672,15 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
                                                            cov->R_lt2, smooth_coop, lambda);
         g_launches += 3;
     } else if (method == FSR_METHOD_TC01) {
-        k_field_backward_iso<true><<<nblk(a.n), kT, 0, c.stream>>>(a);
-        ++g_launches;
+        if (!launch_field_iso_backward_grouped(c, a, true, ctr)) {
+            k_field_backward_iso<true><<<nblk(a.n), kT, 0, c.stream>>>(a);
+            ++g_launches;
+        }
     } else {
-        k_field_backward_iso<false><<<nblk(a.n), kT, 0, c.stream>>>(a);
-        ++g_launches;
+        if (!launch_field_iso_backward_grouped(c, a, false, ctr)) {
+            k_field_backward_iso<false><<<nblk(a.n), kT, 0, c.stream>>>(a);
+            ++g_launches;
+        }
         if (radius_grad_dev) {
             k_radius_grad<<<bb, kT, 0, c.stream>>>(a, ctr, radius_grad_dev);
             ++g_launches;

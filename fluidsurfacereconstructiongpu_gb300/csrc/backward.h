@@ -36,6 +36,11 @@ struct BwdArgs {
     uint32_t cap_band, cap_valid;
 };
 
+// Grouped adjoint of the ZB05 / TC01 fields (field_aniso.cu); adds into a.gx
+// (zeroed).  Returns false (nothing launched) when the grid ratio makes a
+// group too large for shared memory.
+bool launch_field_iso_backward_grouped(const KernelCtx& c, const BwdArgs& a, bool tc01, const Counters* ctr);
+
 void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, const Counters* ctr, int method,
                      float lambda, float R, float* radius_grad_dev, float* out_grad_xyz);
 

@@ -20,6 +20,7 @@
 // Only terms that are exactly zero are skipped; the summation order is the
 // candidate order, the same for every vertex, so results are deterministic.
 #include "kernels.h"
+#include "backward.h"
 
 #include <algorithm>
 
@@ -907,6 +908,156 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
     }
 }
 
+// Adjoint of the ZB05 / TC01 fields (updateScalarFieldValueZB05 cu:230-289,
+// TC01 cu:178-227), grouped like the anisotropic adjoint: a group's vertices
+// with dL/dphi != 0 (and, for ZB05, their (mean - v, weight sum) from the
+// forward) sit in shared memory with one box per 32; the candidates are the
+// particles of the +-1 cell window around the group's cell (the forward's
+// window for each of those vertices), one per thread, and each adds its
+// dL/dx over the active vertices within h with one float4 atomic.
+template <bool TC01>
+__global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, uint32_t vlist_cap, const Counters* ctr)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t nch_cap = (vlist_cap + 31) / 32;
+    float4* av = reinterpret_cast<float4*>(smem);  // active vertices: (v, dL/dphi)
+    float4* am = av + vlist_cap;                    // ZB05: (mean - v, weight sum)
+    float4* cbox = am + (TC01 ? 0 : vlist_cap);     // per 32 of them: lo, hi
+    __shared__ uint32_t s_nv, s_rb[9], s_re[9], s_rp[10];
+    const uint32_t nb = min(ctr->n_band, a.cap_band);
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const float h2 = a.h * a.h, inv_h2 = 1.0f / h2;
+    const float cr = cull_radius(a.h, a.sp.cs), cr2 = cr * cr;
+
+    for (uint32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        if (!a.gkey[g]) continue;  // uniform across the block
+        int c[3], lo[3], hi[3];
+        if (!group_box(g, a.sp, a.sc, a.ratio, c, lo, hi)) continue;
+        const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
+        const int nbox = nx * ny * nz;
+        if (tid == 0) s_nv = 0;
+        __syncthreads();
+        for (int base = 0; base < nbox; base += kBT) {
+            const int i = base + tid;
+            float gv = 0.f;
+            uint32_t rank = 0;
+            int lx = 0, ly = 0, lz = 0;
+            if (i < nbox) {
+                lx = i % nx;
+                ly = (i / nx) % ny;
+                lz = i / (nx * ny);
+                const uint32_t v = lin3(lo[0] + lx, lo[1] + ly, lo[2] + lz, a.sc);
+                if (band_has(a.band, v)) {
+                    rank = band_rank(a.band, v);
+                    if (rank < nb) gv = __ldg(a.gphi + rank);
+                }
+            }
+            const bool act = gv != 0.f;
+            const uint32_t m = __ballot_sync(0xffffffffu, act);
+            uint32_t off = 0;
+            if (lane == 0 && m) off = atomicAdd(&s_nv, __popc(m));
+            off = __shfl_sync(0xffffffffu, off, 0);
+            if (act) {
+                const uint32_t slot = off + __popc(m & ((1u << lane) - 1u));
+                if (slot < vlist_cap) {
+                    av[slot] = make_float4(vpos1(lo[0] + lx, a.sc.min[0], a.sc.cs),
+                                           vpos1(lo[1] + ly, a.sc.min[1], a.sc.cs),
+                                           vpos1(lo[2] + lz, a.sc.min[2], a.sc.cs), gv);
+                    if (!TC01) am[slot] = __ldg(a.mv + rank);
+                }
+            }
+        }
+        // the +-1 window's rows (x-adjacent cells are contiguous in the sorted order)
+        if (tid < 9) {
+            const int x0 = clampi(c[0] - 1, 0, (int)a.sp.res[0] - 1), x1 = clampi(c[0] + 1, 0, (int)a.sp.res[0] - 1);
+            const int y0 = clampi(c[1] - 1, 0, (int)a.sp.res[1] - 1), y1 = clampi(c[1] + 1, 0, (int)a.sp.res[1] - 1);
+            const int z0 = clampi(c[2] - 1, 0, (int)a.sp.res[2] - 1), z1 = clampi(c[2] + 1, 0, (int)a.sp.res[2] - 1);
+            const int yy = y0 + tid % 3, zz = z0 + tid / 3;
+            uint32_t beg = kEmpty, end = 0;
+            if (yy <= y1 && zz <= z1) {
+                const uint32_t c0 = lin3(x0, yy, zz, a.sp);
+                for (int xx = 0; xx <= x1 - x0; ++xx) {
+                    const uint2 r = __ldg(&a.ranges[c0 + xx]);
+                    if (r.x != kEmpty) {
+                        beg = min(beg, r.x);
+                        end = max(end, r.y);
+                    }
+                }
+            }
+            s_rb[tid] = beg;
+            s_re[tid] = end > beg ? end : beg;
+        }
+        __syncthreads();
+        const uint32_t nv = min(s_nv, vlist_cap);
+        if (tid == 0) {
+            uint32_t acc = 0;
+            for (int r = 0; r < 9; ++r) {
+                s_rp[r] = acc;
+                acc += (s_rb[r] == kEmpty) ? 0u : s_re[r] - s_rb[r];
+            }
+            s_rp[9] = acc;
+        }
+        const uint32_t nch = (nv + 31) / 32;
+        for (uint32_t k = tid; k < nch; k += kBT) {
+            float4 l = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), h = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+            for (uint32_t q = 32 * k; q < min(nv, 32 * k + 32); ++q) {
+                const float4 v = av[q];
+                l.x = fminf(l.x, v.x); l.y = fminf(l.y, v.y); l.z = fminf(l.z, v.z);
+                h.x = fmaxf(h.x, v.x); h.y = fmaxf(h.y, v.y); h.z = fmaxf(h.z, v.z);
+            }
+            cbox[2 * k] = l;
+            cbox[2 * k + 1] = h;
+        }
+        __syncthreads();
+        const uint32_t total = nv ? s_rp[9] : 0u;
+        for (uint32_t jj = tid; jj < total; jj += kBT) {
+            int r = 0;
+            while (r < 8 && s_rp[r + 1] <= jj) ++r;
+            const uint32_t j = s_rb[r] + (jj - s_rp[r]);
+            const float4 q = __ldg(&a.sorted[j]);
+            float gx = 0.f, gy = 0.f, gz = 0.f;
+            for (uint32_t k = 0; k < nch; ++k) {
+                if (!(box_dist2(q.x, q.y, q.z, cbox[2 * k], cbox[2 * k + 1]) < cr2)) continue;
+                const uint32_t qe = min(nv, 32 * k + 32);
+                for (uint32_t t = 32 * k; t < qe; ++t) {
+                    const float4 v = av[t];
+                    const float dx = q.x - v.x, dy = q.y - v.y, dz = q.z - v.z;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (TC01) {
+                        if (d2 > h2) continue;
+                        const float tt = d2 * inv_h2 * 0.5f;
+                        const float sg = v.w * (2.f * tt - 1.f) * inv_h2;
+                        gx = fmaf(sg, dx, gx);
+                        gy = fmaf(sg, dy, gy);
+                        gz = fmaf(sg, dz, gz);
+                    } else {
+                        if (d2 >= h2) continue;
+                        const float4 m = am[t];  // mean - v, weight sum
+                        if (!(m.w > 0.f)) continue;
+                        const float ml = sqrtf(fmaf(m.x, m.x, fmaf(m.y, m.y, m.z * m.z)));
+                        if (!(ml > 0.f)) continue;
+                        const float u = 1.0f - d2 * inv_h2;
+                        const float wt = u * u * u;
+                        // d phi / d xbar = (xbar - v) / |xbar - v|; d xbar / d x_j = (w I + (x_j - xbar)
+                        // (dw/dx_j)^T) / W with dw/dx_j = -6 u^2 (x_j - v) / h^2
+                        const float il = v.w / ml;
+                        const float ex = m.x * il, ey = m.y * il, ez = m.z * il;
+                        const float proj = ex * (dx - m.x) + ey * (dy - m.y) + ez * (dz - m.z);
+                        const float k2 = proj * (-6.0f * u * u * inv_h2);
+                        const float iw = 1.0f / m.w;
+                        gx += (wt * ex + k2 * dx) * iw;
+                        gy += (wt * ey + k2 * dy) * iw;
+                        gz += (wt * ez + k2 * dz) * iw;
+                    }
+                }
+            }
+            if (gx != 0.f || gy != 0.f || gz != 0.f) atomicAdd(a.gx + j, make_float4(gx, gy, gz, 0.f));
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 bool launch_field_aniso_backward_grouped(const KernelCtx& c, const AnisoBwdArgs& f, uint32_t ratio,
@@ -968,6 +1119,27 @@ void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
         (groups + kFWarps - 1) / kFWarps, std::max<uint64_t>(1, (uint64_t)c.num_sms * 16 / std::max(1, c.grid_div)));
     k_field_aniso_grouped<<<grid, kFT, 0, c.stream>>>(a, ratio, ctr);
     ++g_launches;
+}
+
+bool launch_field_iso_backward_grouped(const KernelCtx& c, const BwdArgs& a, bool tc01, const Counters* ctr)
+{
+    const uint32_t vcap = (a.ratio + 2) * (a.ratio + 2) * (a.ratio + 2);
+    const size_t smem = sizeof(float4) * vcap * (tc01 ? 1 : 2) + sizeof(float4) * 2 * ((vcap + 31) / 32);
+    if (smem > 200 * 1024) return false;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(k_field_iso_backward_grouped<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_field_iso_backward_grouped<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        configured = true;
+    }
+    const uint64_t groups = (uint64_t)(a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const unsigned grid = (unsigned)std::min<uint64_t>(
+        groups, std::max<uint64_t>(1, (uint64_t)c.num_sms * 8 / std::max(1, c.grid_div)));
+    if (tc01) k_field_iso_backward_grouped<true><<<grid, kBT, smem, c.stream>>>(a, vcap, ctr);
+    else k_field_iso_backward_grouped<false><<<grid, kBT, smem, c.stream>>>(a, vcap, ctr);
+    ++g_launches;
+    return true;
 }
 
 }  // namespace fsr
