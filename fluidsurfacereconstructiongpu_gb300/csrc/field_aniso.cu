@@ -660,7 +660,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             uint32_t count = 0;
             for (; ub < units; ub += per) {
                 const int u = ub + lane;
-                uint32_t rm = 0, v0 = 0;
+                uint32_t rm = 0, v0 = 0, r0 = 0;
                 int x0 = 0, ry = 0, rz = 0;
                 if (lane < per && u < units) {
                     const int seg = u % nseg, row = u / nseg;
@@ -673,6 +673,9 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                     uint64_t bits = __ldg(a.band.bits + w0);
                     if (sh + (uint32_t)wd > 32u) bits |= (uint64_t)__ldg(a.band.bits + w0 + 1) << 32;
                     rm = (uint32_t)(bits >> sh) & (wd >= 32 ? 0xffffffffu : ((1u << wd) - 1u));
+                    // band rank of v0 (whether or not v0 is in the band); bit b of
+                    // rm is vertex v0 + b, so its rank adds the set bits below b
+                    r0 = __ldg(a.band.prefix + w0) + __popc((uint32_t)bits & ((1u << sh) - 1u));
                 }
                 const uint32_t n = __popc(rm);
                 uint32_t x = n;
@@ -689,7 +692,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                     const int bx = __ffs(m) - 1;
                     w.vpos[slot++] = make_float4(vpos1(x0 + bx, a.sc.min[0], a.sc.cs), vpos1(ry, a.sc.min[1], a.sc.cs),
                                                  vpos1(rz, a.sc.min[2], a.sc.cs),
-                                                 __uint_as_float(band_rank(a.band, v0 + (uint32_t)bx)));
+                                                 __uint_as_float(r0 + __popc(rm & ((1u << bx) - 1u))));
                 }
                 count += tot;
             }
