@@ -28,7 +28,6 @@ namespace fsr {
 namespace {
 
 constexpr int kBT = 256;            // threads per block
-constexpr int kWarps = kBT / 32;
 constexpr int kMaxCells = 125;      // 5 x 5 x 5 window
 
 struct GroupArgs {
@@ -296,6 +295,155 @@ __device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
 }
 
+// The layout of a pass of nv <= kPassVerts listed vertices: the pass's box
+// (pl, ph, on every lane), their order in 4 x 4 x 2-vertex bricks (tiles of
+// compact bricks instead of runs of rows: a smaller box per tile, fewer
+// candidates reaching it; a counting sort by brick, the order within a brick
+// is that of the atomics, which changes no result since a vertex's sum does
+// not depend on its tile and culling only skips exact zeros), and the box of
+// each 32-vertex tile.  hist: kPassVerts words of scratch.
+__device__ __forceinline__ void pass_layout(const float4* vpos, uint16_t* order, uint32_t* hist, float4* box,
+                                            uint32_t nv, float inv, int lane, float4& pl, float4& ph)
+{
+    const uint32_t ntiles = (nv + 31) / 32;
+    pl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
+    ph = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+    for (uint32_t q = lane; q < nv; q += 32) {
+        const float4 v = vpos[q];
+        pl.x = fminf(pl.x, v.x); pl.y = fminf(pl.y, v.y); pl.z = fminf(pl.z, v.z);
+        ph.x = fmaxf(ph.x, v.x); ph.y = fmaxf(ph.y, v.y); ph.z = fmaxf(ph.z, v.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        pl.x = fminf(pl.x, __shfl_xor_sync(0xffffffffu, pl.x, o));
+        pl.y = fminf(pl.y, __shfl_xor_sync(0xffffffffu, pl.y, o));
+        pl.z = fminf(pl.z, __shfl_xor_sync(0xffffffffu, pl.z, o));
+        ph.x = fmaxf(ph.x, __shfl_xor_sync(0xffffffffu, ph.x, o));
+        ph.y = fmaxf(ph.y, __shfl_xor_sync(0xffffffffu, ph.y, o));
+        ph.z = fmaxf(ph.z, __shfl_xor_sync(0xffffffffu, ph.z, o));
+    }
+    const int gx = (__float2int_rn((ph.x - pl.x) * inv) >> 2) + 1;
+    const int gy = (__float2int_rn((ph.y - pl.y) * inv) >> 2) + 1;
+    const int gz = (__float2int_rn((ph.z - pl.z) * inv) >> 1) + 1;
+    const int nbins = gx * gy * gz;
+    if (nbins <= kPassVerts) {
+        for (int b = lane; b < nbins; b += 32) hist[b] = 0u;
+        __syncwarp();
+        int key[kPassVerts / 32];
+        uint32_t slot[kPassVerts / 32];
+#pragma unroll
+        for (int k = 0; k < kPassVerts / 32; ++k) {
+            const uint32_t q = lane + 32 * k;
+            key[k] = 0;
+            slot[k] = 0;
+            if (q < nv) {
+                const float4 v = vpos[q];
+                const int ix = __float2int_rn((v.x - pl.x) * inv) >> 2;
+                const int iy = __float2int_rn((v.y - pl.y) * inv) >> 2;
+                const int iz = __float2int_rn((v.z - pl.z) * inv) >> 1;
+                key[k] = min(ix, gx - 1) + gx * (min(iy, gy - 1) + gy * min(iz, gz - 1));
+                slot[k] = atomicAdd(hist + key[k], 1u);
+            }
+        }
+        __syncwarp();
+        // exclusive scan of the bins, lane by lane in blocks of nbins / 32
+        const int per = (nbins + 31) / 32;
+        uint32_t tot = 0;
+        for (int b = lane * per; b < min(nbins, lane * per + per); ++b) tot += hist[b];
+        uint32_t x = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        uint32_t run = x - tot;
+        __syncwarp();
+        for (int b = lane * per; b < min(nbins, lane * per + per); ++b) {
+            const uint32_t hcount = hist[b];
+            hist[b] = run;
+            run += hcount;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < kPassVerts / 32; ++k) {
+            const uint32_t q = lane + 32 * k;
+            if (q < nv) order[hist[key[k]] + slot[k]] = (uint16_t)q;
+        }
+    } else {
+        for (uint32_t q = lane; q < nv; q += 32) order[q] = (uint16_t)q;
+    }
+    __syncwarp();
+    if ((uint32_t)lane < ntiles) {
+        float4 tl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), th = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+        for (uint32_t q = 32 * lane; q < min(nv, 32 * lane + 32); ++q) {
+            const float4 v = vpos[order[q]];
+            tl.x = fminf(tl.x, v.x); tl.y = fminf(tl.y, v.y); tl.z = fminf(tl.z, v.z);
+            th.x = fmaxf(th.x, v.x); th.y = fmaxf(th.y, v.y); th.z = fmaxf(th.z, v.z);
+        }
+        box[2 * lane] = tl;
+        box[2 * lane + 1] = th;
+    }
+    __syncwarp();
+}
+
+// The band vertices of a group's index box [lo, hi), listed into vpos as
+// (position, band rank) by row segments of at most 32 vertices (two bitset
+// words), `per` segments per step so that one step adds at most kPassVerts
+// vertices; pass(count) runs whenever the next step would not fit, and at
+// the end.
+template <class PassFn>
+__device__ __forceinline__ void list_band_vertices(const Grid& sc, const BandView& band, const int lo[3],
+                                                   const int hi[3], float4* vpos, int lane, PassFn&& pass)
+{
+    const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
+    const int nseg = (nx + 31) / 32;
+    const int units = ny * nz * nseg;
+    const int per = max(1, min(32, kPassVerts / min(nx, 32)));
+    int ub = 0;
+    while (ub < units) {
+        uint32_t count = 0;
+        for (; ub < units; ub += per) {
+            const int u = ub + lane;
+            uint32_t rm = 0, v0 = 0, r0 = 0;
+            int x0 = 0, ry = 0, rz = 0;
+            if (lane < per && u < units) {
+                const int seg = u % nseg, row = u / nseg;
+                x0 = lo[0] + 32 * seg;
+                const int wd = min(32, hi[0] - x0);
+                ry = lo[1] + row % ny;
+                rz = lo[2] + row / ny;
+                v0 = lin3(x0, ry, rz, sc);
+                const uint32_t w0 = v0 >> 5, sh = v0 & 31u;
+                uint64_t bits = __ldg(band.bits + w0);
+                if (sh + (uint32_t)wd > 32u) bits |= (uint64_t)__ldg(band.bits + w0 + 1) << 32;
+                rm = (uint32_t)(bits >> sh) & (wd >= 32 ? 0xffffffffu : ((1u << wd) - 1u));
+                // band rank of v0 (whether or not v0 is in the band); bit b of
+                // rm is vertex v0 + b, so its rank adds the set bits below b
+                r0 = __ldg(band.prefix + w0) + __popc((uint32_t)bits & ((1u << sh) - 1u));
+            }
+            const uint32_t n = __popc(rm);
+            uint32_t x = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            const uint32_t tot = __shfl_sync(0xffffffffu, x, 31);
+            // (tot <= kPassVerts by the choice of `per`: an empty pass always takes the step)
+            if (count > 0 && count + tot > (uint32_t)kPassVerts) break;  // run the pass, then this step again
+            uint32_t slot = count + x - n;
+            for (uint32_t m = rm; m; m &= m - 1u) {
+                const int bx = __ffs(m) - 1;
+                vpos[slot++] = make_float4(vpos1(x0 + bx, sc.min[0], sc.cs), vpos1(ry, sc.min[1], sc.cs),
+                                           vpos1(rz, sc.min[2], sc.cs), __uint_as_float(r0 + __popc(rm & ((1u << bx) - 1u))));
+            }
+            count += tot;
+        }
+        __syncwarp();
+        if (count > 0) pass(count);
+    }
+}
+
 // The unscaled kernel's part of the field at vertex v, sum_j c_j (1 - |x_j -
 // v|^2)^3 over the group's non-involved candidates j, is one polynomial in
 // v for the whole group when every candidate is inside the support of every
@@ -391,7 +539,6 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
         if (g >= ngroups) break;
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
-        const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
         bool tables = false;
         uint32_t total = 0;
 
@@ -431,94 +578,10 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 __syncwarp();
             }
             const uint32_t ntiles = (nv + 31) / 32;
-            // the pass's box
-            float4 pl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), ph = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
-            for (uint32_t q = lane; q < nv; q += 32) {
-                const float4 v = w.vpos[q];
-                pl.x = fminf(pl.x, v.x); pl.y = fminf(pl.y, v.y); pl.z = fminf(pl.z, v.z);
-                ph.x = fmaxf(ph.x, v.x); ph.y = fmaxf(ph.y, v.y); ph.z = fmaxf(ph.z, v.z);
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                pl.x = fminf(pl.x, __shfl_xor_sync(0xffffffffu, pl.x, o));
-                pl.y = fminf(pl.y, __shfl_xor_sync(0xffffffffu, pl.y, o));
-                pl.z = fminf(pl.z, __shfl_xor_sync(0xffffffffu, pl.z, o));
-                ph.x = fmaxf(ph.x, __shfl_xor_sync(0xffffffffu, ph.x, o));
-                ph.y = fmaxf(ph.y, __shfl_xor_sync(0xffffffffu, ph.y, o));
-                ph.z = fmaxf(ph.z, __shfl_xor_sync(0xffffffffu, ph.z, o));
-            }
-            // tiles of compact bricks (4 x 4 x 2 vertices) instead of runs of
-            // rows: a smaller box per tile, fewer candidates reaching it.  A
-            // counting sort by brick; the order within a brick is that of the
-            // atomics, which changes no result (a vertex's sum does not
-            // depend on its tile, culling only skips exact zeros)
-            {
-                const float inv = 1.0f / a.sc.cs;
-                const int gx = (__float2int_rn((ph.x - pl.x) * inv) >> 2) + 1;
-                const int gy = (__float2int_rn((ph.y - pl.y) * inv) >> 2) + 1;
-                const int gz = (__float2int_rn((ph.z - pl.z) * inv) >> 1) + 1;
-                const int nbins = gx * gy * gz;
-                uint32_t* hist = reinterpret_cast<uint32_t*>(&w.psum[0][0]);  // psum is zeroed below
-                if (nbins <= kPassTiles * 32) {
-                    for (int b = lane; b < nbins; b += 32) hist[b] = 0u;
-                    __syncwarp();
-                    int key[kPassVerts / 32];
-                    uint32_t slot[kPassVerts / 32];
-#pragma unroll
-                    for (int k = 0; k < kPassVerts / 32; ++k) {
-                        const uint32_t q = lane + 32 * k;
-                        key[k] = 0;
-                        slot[k] = 0;
-                        if (q < nv) {
-                            const float4 v = w.vpos[q];
-                            const int ix = __float2int_rn((v.x - pl.x) * inv) >> 2;
-                            const int iy = __float2int_rn((v.y - pl.y) * inv) >> 2;
-                            const int iz = __float2int_rn((v.z - pl.z) * inv) >> 1;
-                            key[k] = min(ix, gx - 1) + gx * (min(iy, gy - 1) + gy * min(iz, gz - 1));
-                            slot[k] = atomicAdd(hist + key[k], 1u);
-                        }
-                    }
-                    __syncwarp();
-                    // exclusive scan of the bins, lane by lane in blocks of nbins / 32
-                    const int per = (nbins + 31) / 32;
-                    uint32_t tot = 0;
-                    for (int b = lane * per; b < min(nbins, lane * per + per); ++b) tot += hist[b];
-                    uint32_t x = tot;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                        if (lane >= o) x += y;
-                    }
-                    uint32_t run = x - tot;
-                    __syncwarp();
-                    for (int b = lane * per; b < min(nbins, lane * per + per); ++b) {
-                        const uint32_t hcount = hist[b];
-                        hist[b] = run;
-                        run += hcount;
-                    }
-                    __syncwarp();
-#pragma unroll
-                    for (int k = 0; k < kPassVerts / 32; ++k) {
-                        const uint32_t q = lane + 32 * k;
-                        if (q < nv) w.order[hist[key[k]] + slot[k]] = (uint16_t)q;
-                    }
-                } else {
-                    for (uint32_t q = lane; q < nv; q += 32) w.order[q] = (uint16_t)q;
-                }
-                __syncwarp();
-            }
-            // tile boxes (lane t: tile t)
-            if ((uint32_t)lane < ntiles) {
-                float4 tl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), th = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
-                for (uint32_t q = 32 * lane; q < min(nv, 32 * lane + 32); ++q) {
-                    const float4 v = w.vpos[w.order[q]];
-                    tl.x = fminf(tl.x, v.x); tl.y = fminf(tl.y, v.y); tl.z = fminf(tl.z, v.z);
-                    th.x = fmaxf(th.x, v.x); th.y = fmaxf(th.y, v.y); th.z = fmaxf(th.z, v.z);
-                }
-                w.box[2 * lane] = tl;
-                w.box[2 * lane + 1] = th;
-            }
-            __syncwarp();
+            // the pass's box, brick order and tile boxes
+            float4 pl, ph;
+            pass_layout(w.vpos, w.order, reinterpret_cast<uint32_t*>(&w.psum[0][0]), w.box, nv, 1.0f / a.sc.cs, lane,
+                        pl, ph);  // psum is zeroed below
             // two sums per vertex: the involved particles' terms, then the
             // non-involved particles' (the unscaled kernel: about 1e-7 each,
             // thousands of them), added among themselves and joined at the
@@ -649,56 +712,177 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             __syncwarp();
         };
 
-        // band vertices of the box by row segments of at most 32 vertices (two
-        // bitset words), `per` segments per step so that one step adds at most
-        // kPassVerts vertices; a pass runs whenever the next step would not fit
-        const int nseg = (nx + 31) / 32;
-        const int units = ny * nz * nseg;
-        const int per = max(1, min(32, kPassVerts / min(nx, 32)));
-        int ub = 0;
-        while (ub < units) {
-            uint32_t count = 0;
-            for (; ub < units; ub += per) {
-                const int u = ub + lane;
-                uint32_t rm = 0, v0 = 0, r0 = 0;
-                int x0 = 0, ry = 0, rz = 0;
-                if (lane < per && u < units) {
-                    const int seg = u % nseg, row = u / nseg;
-                    x0 = lo[0] + 32 * seg;
-                    const int wd = min(32, hi[0] - x0);
-                    ry = lo[1] + row % ny;
-                    rz = lo[2] + row / ny;
-                    v0 = lin3(x0, ry, rz, a.sc);
-                    const uint32_t w0 = v0 >> 5, sh = v0 & 31u;
-                    uint64_t bits = __ldg(a.band.bits + w0);
-                    if (sh + (uint32_t)wd > 32u) bits |= (uint64_t)__ldg(a.band.bits + w0 + 1) << 32;
-                    rm = (uint32_t)(bits >> sh) & (wd >= 32 ? 0xffffffffu : ((1u << wd) - 1u));
-                    // band rank of v0 (whether or not v0 is in the band); bit b of
-                    // rm is vertex v0 + b, so its rank adds the set bits below b
-                    r0 = __ldg(a.band.prefix + w0) + __popc((uint32_t)bits & ((1u << sh) - 1u));
+        list_band_vertices(a.sc, a.band, lo, hi, w.vpos, lane, pass);
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- ZB05 / TC01
+// updateScalarFieldValueZB05 (cu:230-289) and updateScalarFieldValueTC01
+// (cu:178-227) grouped like the anisotropic field: a band vertex's
+// candidates are the particles of the +-1 cells around its cell, the same for
+// every vertex of the cell, so one warp streams them once per pass of up to
+// 256 vertices and, per brick tile, evaluates only those within h of the
+// tile's box.  Each vertex sums its terms in window order (cells z, y, x,
+// particles in sorted order); candidates of the window cells the per-vertex
+// walk narrows away lie beyond h and add nothing.
+struct IsoSlice {
+    float4 rec[32];                // the current chunk's candidates, one per lane
+    float4 vpos[kPassVerts];       // the pass's band vertices: position, band rank (bits)
+    float4 box[2 * kPassTiles];    // per tile: lo, hi
+    float sum[4][kPassTiles][32];  // per vertex: weight sum, then (ZB05) sum w (x - v)
+    uint16_t order[kPassVerts];    // the pass's vertices in brick order
+    uint32_t rb[9], rp[10];        // the window's rows: first particle, prefix of lengths
+};
+
+__device__ __forceinline__ bool within(float4 q, float4 lo, float4 hi, float r2)
+{
+    const float gx = fmaxf(0.f, fmaxf(lo.x - q.x, q.x - hi.x));
+    const float gy = fmaxf(0.f, fmaxf(lo.y - q.y, q.y - hi.y));
+    const float gz = fmaxf(0.f, fmaxf(lo.z - q.z, q.z - hi.z));
+    return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r2;
+}
+
+template <bool TC01>
+__global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandView band, uint32_t ratio, Counters* ctr)
+{
+    __shared__ IsoSlice slices[kFWarps];
+    const int lane = threadIdx.x & 31;
+    IsoSlice& w = slices[threadIdx.x >> 5];
+    const uint32_t nb = min(ctr->n_band, a.cap);
+    const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const float cr = cull_radius(a.h, a.sp.cs), cr2 = cr * cr;
+    constexpr int kSums = TC01 ? 1 : 4;
+
+    for (;;) {
+        uint32_t g = 0;
+        if (lane == 0) g = atomicAdd(&ctr->work_field, 1u);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g >= ngroups) break;
+        int c[3], lo[3], hi[3];
+        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
+        // rows of the +-1 window (clamped as window() clamps), z then y
+        if (lane < 9) {
+            const int x0 = clampi(c[0] - 1, 0, (int)a.sp.res[0] - 1), x1 = clampi(c[0] + 1, 0, (int)a.sp.res[0] - 1);
+            const int y0 = clampi(c[1] - 1, 0, (int)a.sp.res[1] - 1), y1 = clampi(c[1] + 1, 0, (int)a.sp.res[1] - 1);
+            const int z0 = clampi(c[2] - 1, 0, (int)a.sp.res[2] - 1), z1 = clampi(c[2] + 1, 0, (int)a.sp.res[2] - 1);
+            const int yy = y0 + lane % 3, zz = z0 + lane / 3;
+            uint32_t beg = kEmpty, end = 0;
+            if (yy <= y1 && zz <= z1) {
+                const uint32_t c0 = lin3(x0, yy, zz, a.sp);
+                for (int xx = 0; xx <= x1 - x0; ++xx) {
+                    const uint2 r = __ldg(&a.ranges[c0 + xx]);
+                    if (r.x != kEmpty) {
+                        beg = min(beg, r.x);
+                        end = max(end, r.y);
+                    }
                 }
-                const uint32_t n = __popc(rm);
-                uint32_t x = n;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-                    if (lane >= o) x += y;
+            }
+            w.rb[lane] = beg;
+            w.rp[lane + 1] = beg == kEmpty ? 0u : end - beg;  // lengths for now
+        }
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t acc = 0;
+            for (int r = 0; r < 9; ++r) {
+                const uint32_t len = w.rp[r + 1];
+                w.rp[r] = acc;
+                acc += len;
+            }
+            w.rp[9] = acc;
+        }
+        __syncwarp();
+        const uint32_t total = w.rp[9];
+
+        auto pass = [&](uint32_t nv) {
+            float4 pl, ph;
+            pass_layout(w.vpos, w.order, reinterpret_cast<uint32_t*>(&w.sum[0][0][0]), w.box, nv, 1.0f / a.sc.cs, lane,
+                        pl, ph);  // the sums are zeroed next
+            const uint32_t ntiles = (nv + 31) / 32;
+            for (int k = 0; k < kSums; ++k)
+                for (int t = 0; t < kPassTiles; ++t) w.sum[k][t][lane] = 0.f;
+            __syncwarp();
+            for (uint32_t cb = 0; cb < total; cb += 32) {
+                const uint32_t j = cb + lane;
+                bool keep = false;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < total) {
+                    int r = 0;
+                    while (r < 8 && w.rp[r + 1] <= j) ++r;
+                    q = __ldg(&a.sorted[w.rb[r] + (j - w.rp[r])]);
+                    keep = within(q, pl, ph, cr2);
+                    if (keep) w.rec[lane] = q;
                 }
-                const uint32_t tot = __shfl_sync(0xffffffffu, x, 31);
-                // (tot <= kPassVerts by the choice of `per`: an empty pass always takes the step)
-                if (count > 0 && count + tot > (uint32_t)kPassVerts) break;  // run the pass, then this step again
-                uint32_t slot = count + x - n;
-                for (uint32_t m = rm; m; m &= m - 1u) {
-                    const int bx = __ffs(m) - 1;
-                    w.vpos[slot++] = make_float4(vpos1(x0 + bx, a.sc.min[0], a.sc.cs), vpos1(ry, a.sc.min[1], a.sc.cs),
-                                                 vpos1(rz, a.sc.min[2], a.sc.cs),
-                                                 __uint_as_float(r0 + __popc(rm & ((1u << bx) - 1u))));
+                const uint32_t any = __ballot_sync(0xffffffffu, keep);
+                __syncwarp();
+                if (any) {
+#pragma unroll 1
+                    for (int t = 0; t < kPassTiles; ++t) {
+                        if ((uint32_t)t >= ntiles) break;
+                        const uint32_t m = __ballot_sync(0xffffffffu, keep && within(q, w.box[2 * t], w.box[2 * t + 1], cr2));
+                        const uint32_t v = 32 * t + lane;
+                        if (m && v < nv) {
+                            const float4 vp = w.vpos[w.order[v]];
+                            float ws = w.sum[0][t][lane];
+                            float ax = 0.f, ay = 0.f, az = 0.f;
+                            if (!TC01) {
+                                ax = w.sum[1][t][lane];
+                                ay = w.sum[2][t][lane];
+                                az = w.sum[3][t][lane];
+                            }
+                            for (uint32_t mm = m; mm; mm &= mm - 1u) {
+                                const float4 qq = w.rec[__ffs(mm) - 1];
+                                const float dx = qq.x - vp.x, dy = qq.y - vp.y, dz = qq.z - vp.z;
+                                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                if (TC01) {
+                                    if (d2 <= a.h2) {
+                                        const float u = d2 * a.inv_h2 * 0.5f;
+                                        ws += u * u - u + 0.25f;
+                                    }
+                                } else if (d2 < a.h2) {
+                                    const float u = 1.0f - d2 * a.inv_h2;
+                                    const float wt = u * u * u;
+                                    ws += wt;
+                                    ax = fmaf(dx, wt, ax);
+                                    ay = fmaf(dy, wt, ay);
+                                    az = fmaf(dz, wt, az);
+                                }
+                            }
+                            w.sum[0][t][lane] = ws;
+                            if (!TC01) {
+                                w.sum[1][t][lane] = ax;
+                                w.sum[2][t][lane] = ay;
+                                w.sum[3][t][lane] = az;
+                            }
+                        }
+                    }
                 }
-                count += tot;
+                __syncwarp();
+            }
+            for (int t = 0; t < (int)ntiles; ++t) {
+                const uint32_t v = 32 * t + lane;
+                if (v < nv) {
+                    const uint32_t rank = __float_as_uint(w.vpos[w.order[v]].w);
+                    if (rank < nb) {
+                        const float ws = w.sum[0][t][lane];
+                        if (TC01) {
+                            a.phi[rank] = ws;
+                        } else {
+                            const float ax = w.sum[1][t][lane], ay = w.sum[2][t][lane], az = w.sum[3][t][lane];
+                            // |v - sum w p / sum w| = |sum w (p - v)| / sum w; a vertex with no
+                            // weight keeps 0, the reference's memset value (cu:284)
+                            a.phi[rank] = ws > 0.f ? sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az))) / ws - a.rp : 0.f;
+                            if (a.mv) {
+                                const float inv = ws > 0.f ? 1.0f / ws : 0.f;
+                                a.mv[rank] = make_float4(ax * inv, ay * inv, az * inv, ws);
+                            }
+                        }
+                    }
+                }
             }
             __syncwarp();
-            if (count > 0) pass(count);
-        }
+        };
+        list_band_vertices(a.sc, band, lo, hi, w.vpos, lane, pass);
         __syncwarp();
     }
 }
@@ -922,7 +1106,6 @@ template <bool TC01>
 __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, uint32_t vlist_cap, const Counters* ctr)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t nch_cap = (vlist_cap + 31) / 32;
     float4* av = reinterpret_cast<float4*>(smem);  // active vertices: (v, dL/dphi)
     float4* am = av + vlist_cap;                    // ZB05: (mean - v, weight sum)
     float4* cbox = am + (TC01 ? 0 : vlist_cap);     // per 32 of them: lo, hi
@@ -1143,6 +1326,17 @@ bool launch_field_iso_backward_grouped(const KernelCtx& c, const BwdArgs& a, boo
     else k_field_iso_backward_grouped<false><<<grid, kBT, smem, c.stream>>>(a, vcap, ctr);
     ++g_launches;
     return true;
+}
+
+void launch_field_iso_grouped(const KernelCtx& c, bool tc01, const IsoFieldArgs& f, const BandView& band, uint32_t ratio,
+                              Counters* ctr)
+{
+    const uint64_t groups = (uint64_t)(f.sp.res[0] + 1) * (f.sp.res[1] + 1) * (f.sp.res[2] + 1);
+    const unsigned grid = (unsigned)std::min<uint64_t>(
+        (groups + kFWarps - 1) / kFWarps, std::max<uint64_t>(1, (uint64_t)c.num_sms * 16 / std::max(1, c.grid_div)));
+    if (tc01) k_field_iso_grouped<true><<<grid, kFT, 0, c.stream>>>(f, band, ratio, ctr);
+    else k_field_iso_grouped<false><<<grid, kFT, 0, c.stream>>>(f, band, ratio, ctr);
+    ++g_launches;
 }
 
 }  // namespace fsr

@@ -303,135 +303,6 @@ __global__ void k_band_list(const uint32_t* __restrict__ bits, const uint32_t* _
     }
 }
 
-// ------------------------------------------------------------ isotropic fields
-// updateScalarFieldValueZB05 (cu:230-289) and updateScalarFieldValueTC01
-// (cu:178-227): +-1 cell window around the vertex's cell.  A ZB05 vertex
-// with no weight keeps 0, the reference's memset value (cu:284).
-template <Field F>
-__global__ void __launch_bounds__(kThreads) k_field_iso(IsoFieldArgs a, const Counters* ctr)
-{
-    __shared__ float4 s_q[kThreads];   // 32 staged candidates per warp
-    __shared__ uint32_t s_c[kThreads]; // their cells' x index
-    const uint32_t nb = min(ctr->n_band, a.cap);
-    const int lane = threadIdx.x & 31;
-    float4* sq = s_q + (threadIdx.x & ~31u);
-    uint32_t* sc = s_c + (threadIdx.x & ~31u);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    // warp-uniform loop: lanes beyond the band take part in the warp's work
-    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < nb; base += stride) {
-        const uint32_t t = base + lane;
-        const bool active = t < nb;
-        uint32_t x = 0, y = 0, z = 0;
-        if (active) unlin3(a.sv[t], a.sc, x, y, z);
-        const float vx = vpos1(x, a.sc.min[0], a.sc.cs), vy = vpos1(y, a.sc.min[1], a.sc.cs),
-                    vz = vpos1(z, a.sc.min[2], a.sc.cs);
-        // only particles within h contribute: narrow the +-1 window to h
-        const Window w = narrow(window(cell1(vx, a.sp.min[0], a.sp.cs), cell1(vy, a.sp.min[1], a.sp.cs),
-                                       cell1(vz, a.sp.min[2], a.sp.cs), 1, a.sp),
-                                vx, vy, vz, cull_radius(a.h, a.sp.cs), a.sp);
-        float ws = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
-        auto add = [&](const float4& q) {
-            const float dx = q.x - vx, dy = q.y - vy, dz = q.z - vz;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            if (F == Field::kZB05) {
-                // weighted mean taken as an offset from the vertex:
-                // |v - sum w p / sum w| = |sum w (p - v)| / sum w, the
-                // same value with FP32 error relative to h, not to |p|
-                if (d2 < a.h2) {
-                    const float u = 1.0f - d2 * a.inv_h2;
-                    const float wt = u * u * u;
-                    ws += wt;
-                    ax = fmaf(dx, wt, ax);
-                    ay = fmaf(dy, wt, ay);
-                    az = fmaf(dz, wt, az);
-                }
-            } else {
-                if (d2 <= a.h2) {
-                    const float u = d2 * a.inv_h2 * 0.5f;
-                    ws += u * u - u + 0.25f;
-                }
-            }
-        };
-        auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
-            // cells xx = x0..x1 of this row are contiguous in the sorted array
-            const uint32_t c0 = lin3(x0, yy, zz, a.sp);
-            beg = kEmpty;
-            end = 0;
-            for (int xx = 0; xx <= x1 - x0; ++xx) {
-                const uint2 r = __ldg(&a.ranges[c0 + xx]);
-                if (r.x != kEmpty) {
-                    beg = min(beg, r.x);
-                    end = max(end, r.y);
-                }
-            }
-        };
-        // A warp whose windows span at most 4 cells per axis walks their
-        // union together, 32 staged candidates at a time.  Each lane takes a
-        // candidate only if its cell lies in the lane's own window (x from the
-        // particle's key, y and z from the row), so every vertex sees exactly
-        // its window's particles in window order, as in the per-lane walk.
-        int ulo[3], uhi[3];
-        bool compact = true;
-#pragma unroll
-        for (int ax3 = 0; ax3 < 3; ++ax3) {
-            ulo[ax3] = (int)__reduce_min_sync(0xffffffffu, active ? (unsigned)w.lo[ax3] : 0x7fffffffu);
-            uhi[ax3] = (int)__reduce_max_sync(0xffffffffu, active ? (unsigned)(w.hi[ax3] + 1) : 0u) - 1;
-            compact = compact && uhi[ax3] - ulo[ax3] <= 3;
-        }
-        if (compact) {
-            // particles beyond h of every lane's vertex are dropped at staging
-            const WarpBox box = warp_box(active, vx, vy, vz, cull_radius(a.h, a.sp.cs));
-            for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
-                for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
-                    const bool row_in = active && zz >= w.lo[2] && zz <= w.hi[2] && yy >= w.lo[1] && yy <= w.hi[1];
-                    if (!__any_sync(0xffffffffu, row_in)) continue;
-                    uint32_t beg, end;
-                    row_range(ulo[0], uhi[0], yy, zz, beg, end);
-                    for (uint32_t b = beg; b < end; b += 32) {
-                        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                        bool keep = false;
-                        if (b + lane < end) {
-                            q = __ldg(&a.sorted[b + lane]);
-                            keep = box.holds(q);
-                        }
-                        const uint32_t mk = __ballot_sync(0xffffffffu, keep);
-                        if (keep) {
-                            const uint32_t slot = __popc(mk & ((1u << lane) - 1u));
-                            sq[slot] = q;
-                            sc[slot] = __ldg(&a.skeys[b + lane]) % a.sp.res[0];
-                        }
-                        __syncwarp();
-                        const uint32_t cnt = __popc(mk);
-                        if (row_in)
-                            for (uint32_t k = 0; k < cnt; ++k) {
-                                const int cx = (int)sc[k];
-                                if (cx >= w.lo[0] && cx <= w.hi[0]) add(sq[k]);
-                            }
-                        __syncwarp();
-                    }
-                }
-        } else if (active) {
-            for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-                for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-                    uint32_t beg, end;
-                    row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
-                    for (uint32_t i = beg; i < end; ++i) add(__ldg(&a.sorted[i]));
-                }
-        }
-        if (!active) continue;
-        float phi;
-        if (F == Field::kZB05) {
-            phi = ws > 0.f ? sqrtf(fmaf(ax, ax, fmaf(ay, ay, az * az))) / ws - a.rp : 0.f;
-            if (a.mv) {
-                const float inv = ws > 0.f ? 1.0f / ws : 0.f;
-                a.mv[t] = make_float4(ax * inv, ay * inv, az * inv, ws);
-            }
-        } else {
-            phi = ws;
-        }
-        a.phi[t] = phi;
-    }
-}
 
 // Stages the warp's next chunk of candidates [base, end): the ones inside
 // the box go to sq in their order; returns how many.
@@ -964,13 +835,6 @@ void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* 
     ++g_launches;
 }
 
-void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr)
-{
-    const unsigned g = persistent_blocks(c, a.cap, 16);
-    if (f == Field::kTC01) k_field_iso<Field::kTC01><<<g, kThreads, 0, c.stream>>>(a, ctr);
-    else k_field_iso<Field::kZB05><<<g, kThreads, 0, c.stream>>>(a, ctr);
-    ++g_launches;
-}
 
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
                    float R, float lambda, float mass, float4* mean, float4* smoothed)

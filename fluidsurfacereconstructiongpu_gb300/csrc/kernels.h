@@ -61,7 +61,10 @@ struct IsoFieldArgs {
     float h, h2, inv_h2, rp;
     uint32_t cap;
 };
-void launch_field_iso(const KernelCtx& c, Field f, const IsoFieldArgs& a, Counters* ctr);
+// updateScalarFieldValueZB05 / TC01 (cu:178-289), grouped by window like the
+// anisotropic field (field_aniso.cu).
+void launch_field_iso_grouped(const KernelCtx& c, bool tc01, const IsoFieldArgs& a, const BandView& band,
+                              uint32_t ratio, Counters* ctr);
 
 // Yu13 smoothing: mean (exact FP32) and smoothed position with m/rho in w.
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,

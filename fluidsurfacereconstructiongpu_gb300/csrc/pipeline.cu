@@ -406,7 +406,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.rp = hdr.particle_radius;
         fa.mv = p.method == FSR_METHOD_TC01 ? nullptr : (float4*)h->mv.ptr;
         fa.cap = h->cap_band;
-        launch_field_iso(kc, p.method == FSR_METHOD_TC01 ? Field::kTC01 : Field::kZB05, fa, ctr);
+        launch_field_iso_grouped(kc, p.method == FSR_METHOD_TC01, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr);
     }
     mark(7);
 
