@@ -187,54 +187,142 @@ __global__ void k_involved_cells(Grid sp, const uint8_t* __restrict__ occ, const
 // cuh:324-334).  The decision |grad c| > 3 depends on a sum, so the sum is
 // taken in the reference's order with the reference's roundings (FP64 where
 // the source promotes).
-__global__ void k_colorfield(const float4* __restrict__ sorted, uint32_t n, const uint2* __restrict__ ranges,
-                             Grid sp, float h, float h_lt2, double k_spiky, float mass, uint8_t* __restrict__ psurf)
+__global__ void __launch_bounds__(kThreads) k_colorfield(const float4* __restrict__ sorted, uint32_t n,
+                                                         const uint2* __restrict__ ranges,
+                                                         const uint32_t* __restrict__ skeys, Grid sp, float h,
+                                                         float h_rcp, float h_lt2, double k_spiky, float mass,
+                                                         uint8_t* __restrict__ psurf)
 {
+    __shared__ float4 s_q[kThreads];    // staged candidates, per warp
+    __shared__ float s_mr[kThreads];    // their m / rho
+    __shared__ uint32_t s_cx[kThreads]; // their cells' x index
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const float4 p = sorted[t];
+    const bool active = t < n;
+    if (__all_sync(0xffffffffu, !active)) return;
+    const int lane = threadIdx.x & 31;
+    const uint32_t wb = threadIdx.x & ~31u;
+    const float4 p = active ? sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
     const Window w = window(cell1(p.x, sp.min[0], sp.cs), cell1(p.y, sp.min[1], sp.cs),
                             cell1(p.z, sp.min[2], sp.cs), 1, sp);
-    uint32_t nn = 0;
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    // the particles of a row of x-adjacent cells are contiguous in sorted order
-    for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
-        for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
-            const uint32_t c0 = lin3(w.lo[0], yy, zz, sp);
-            uint32_t beg = kEmpty, end = 0;
-            for (int xx = 0; xx <= w.hi[0] - w.lo[0]; ++xx) {
-                const uint2 r = __ldg(&ranges[c0 + xx]);
-                if (r.x != kEmpty) {
-                    beg = min(beg, r.x);
-                    end = max(end, r.y);
-                }
-            }
-            for (uint32_t i = beg; i < end; ++i) {
-                const float4 q = __ldg(&sorted[i]);
-                float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
-                const float d2 = dot3_rn(rx, ry, rz);
-                if (!(d2 > 0.0f)) continue;
-                ++nn;
-                // d >= h: the gradient is 0 and the +0 / -0 terms leave the
-                // sums (never -0) unchanged
-                if (!(d2 < h_lt2)) continue;
-                const float d = __fsqrt_rn(d2);
-                // x = float(1.0 - (double)(d / h)): the double difference of 1
-                // and a float is exact, so rounding it to float is the
-                // correctly rounded FP32 difference (no FP64 work needed)
-                const float x = __fsub_rn(1.0f, __fdiv_rn(d, h));
-                const double xd = (double)x;
-                const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, xd), xd));
-                const float inv = __fdiv_rn(1.0f, d);
-                rx = __fmul_rn(rx, inv);
-                ry = __fmul_rn(ry, inv);
-                rz = __fmul_rn(rz, inv);
-                const float coef = __fmul_rn(__fdiv_rn(mass, q.w), grad);
-                sx = __fadd_rn(sx, __fmul_rn(coef, rx));
-                sy = __fadd_rn(sy, __fmul_rn(coef, ry));
-                sz = __fadd_rn(sz, __fmul_rn(coef, rz));
+    // a neighbour at squared distance 0 < d2 < h^2 (the gradient is 0 at d >= h,
+    // and +0 / -0 terms leave the sums, never -0, unchanged)
+    auto add = [&](float4 q, float d2, float m_rho) {
+        float rx = __fsub_rn(p.x, q.x), ry = __fsub_rn(p.y, q.y), rz = __fsub_rn(p.z, q.z);
+        const float d = __fsqrt_rn(d2);
+        // x = float(1.0 - (double)(d / h)): the double difference of 1 and a
+        // float is exact, so rounding it to float is the correctly rounded
+        // FP32 difference (no FP64 work needed)
+        const float x = __fsub_rn(1.0f, div_exact(d, h, h_rcp));
+        const double xd = (double)x;
+        const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, xd), xd));
+        const float inv = __fdiv_rn(1.0f, d);
+        rx = __fmul_rn(rx, inv);
+        ry = __fmul_rn(ry, inv);
+        rz = __fmul_rn(rz, inv);
+        const float coef = __fmul_rn(m_rho, grad);
+        sx = __fadd_rn(sx, __fmul_rn(coef, rx));
+        sy = __fadd_rn(sy, __fmul_rn(coef, ry));
+        sz = __fadd_rn(sz, __fmul_rn(coef, rz));
+    };
+    auto dist2 = [&](const float4& q) {
+        return dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+    };
+    auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end, uint32_t& cnt) {
+        // the particles of a row of x-adjacent cells are contiguous in sorted order
+        const uint32_t c0 = lin3(x0, yy, zz, sp);
+        beg = kEmpty;
+        end = 0;
+        cnt = 0;
+        for (int xx = 0; xx <= x1 - x0; ++xx) {
+            const uint2 r = __ldg(&ranges[c0 + xx]);
+            if (r.x != kEmpty) {
+                beg = min(beg, r.x);
+                end = max(end, r.y);
+                cnt += r.y - r.x;
             }
         }
+    };
+    // nn: the particles of the window at a distance > 0 (the reference counts
+    // every particle of the 27 cells, cu:930-950) = the window's particles
+    // minus those at distance 0 (the particle itself and exact duplicates)
+    uint32_t nn = 0;
+    int ulo[3], uhi[3];
+    bool compact = true;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        ulo[ax] = (int)__reduce_min_sync(0xffffffffu, active ? (unsigned)w.lo[ax] : 0x7fffffffu);
+        uhi[ax] = (int)__reduce_max_sync(0xffffffffu, active ? (unsigned)(w.hi[ax] + 1) : 0u) - 1;
+        compact = compact && uhi[ax] - ulo[ax] <= 4;
+    }
+    if (compact) {
+        // the warp walks the union of its windows; staging drops what lies
+        // beyond h of every lane's particle (zero gradient, and such a
+        // particle is at a distance > 0, counted through the cell counts);
+        // each lane takes the staged particles of its own window in window
+        // order (rows from the loop, x from the cell index)
+        uint32_t in_window = 0, zeros = 0;
+        if (active)
+            for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+                for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                    uint32_t b, e, c;
+                    row_range(w.lo[0], w.hi[0], yy, zz, b, e, c);
+                    in_window += c;
+                }
+        const WarpBox box = warp_box(active, p.x, p.y, p.z, cull_radius(h, sp.cs));
+        for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
+            for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
+                const bool row_in = active && zz >= w.lo[2] && zz <= w.hi[2] && yy >= w.lo[1] && yy <= w.hi[1];
+                if (!__any_sync(0xffffffffu, row_in)) continue;
+                uint32_t beg, end, c;
+                row_range(ulo[0], uhi[0], yy, zz, beg, end, c);
+                for (uint32_t b = beg; b < end; b += 32) {
+                    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                    bool keep = false;
+                    if (b + lane < end) {
+                        q = __ldg(&sorted[b + lane]);
+                        keep = box.holds(q);
+                    }
+                    const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const uint32_t slot = wb + __popc(mk & ((1u << lane) - 1u));
+                        s_q[slot] = q;
+                        s_mr[slot] = __fdiv_rn(mass, q.w);
+                        s_cx[slot] = __ldg(&skeys[b + lane]) % sp.res[0];
+                    }
+                    __syncwarp();
+                    const uint32_t cnt = __popc(mk);
+                    if (row_in)
+                        for (uint32_t k = 0; k < cnt; ++k) {
+                            const int cx = (int)s_cx[wb + k];
+                            if (cx < w.lo[0] || cx > w.hi[0]) continue;
+                            const float4 q2 = s_q[wb + k];
+                            const float d2 = dist2(q2);
+                            if (!(d2 > 0.0f)) {
+                                ++zeros;
+                                continue;
+                            }
+                            if (d2 < h_lt2) add(q2, d2, s_mr[wb + k]);
+                        }
+                    __syncwarp();
+                }
+            }
+        nn = in_window - zeros;
+    } else if (active) {
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                uint32_t beg, end, c;
+                row_range(w.lo[0], w.hi[0], yy, zz, beg, end, c);
+                for (uint32_t i = beg; i < end; ++i) {
+                    const float4 q = __ldg(&sorted[i]);
+                    const float d2 = dist2(q);
+                    if (!(d2 > 0.0f)) continue;
+                    ++nn;
+                    if (d2 < h_lt2) add(q, d2, __fdiv_rn(mass, q.w));
+                }
+            }
+    }
+    if (!active) return;
     const bool s = nn < 25u || __fsqrt_rn(dot3_rn(sx, sy, sz)) > 3.0f;
     psurf[t] = s ? 1 : 0;
 }
@@ -809,13 +897,13 @@ void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* oc
 }
 
 void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges,
-                       const Grid& sp, float h, float h2, float mass, uint8_t* psurf)
+                       const uint32_t* skeys, const Grid& sp, float h, float h2, float mass, uint8_t* psurf)
 {
     if (!n) return;
     // -45 / (pi h^4) exactly as the reference evaluates it in double
     const double k = -45.0 / (3.1415926535 * (double)h2 * (double)h2);
-    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, h, sqrt_threshold(h, false), k, mass,
-                                                           psurf);
+    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, skeys, sp, h, 1.0f / h,
+                                                           sqrt_threshold(h, false), k, mass, psurf);
     ++g_launches;
 }
 

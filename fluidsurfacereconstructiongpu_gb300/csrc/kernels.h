@@ -39,7 +39,7 @@ void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* oc
 
 // Akinci12 colour-field surface flags per sorted particle (u8).
 void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges,
-                       const Grid& sp, float h, float h2, float mass, uint8_t* psurf);
+                       const uint32_t* skeys, const Grid& sp, float h, float h2, float mass, uint8_t* psurf);
 
 // Band stamp around surface particles.  Surface particles are those with
 // psurf[i] != 0 when psurf is given, else those whose cell has surf != 0.

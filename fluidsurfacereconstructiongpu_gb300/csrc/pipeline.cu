@@ -326,7 +326,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     uint8_t* surf = (uint8_t*)h->surf.ptr;
     uint8_t* psurf = akinci ? (uint8_t*)h->psurf.ptr : nullptr;
     if (akinci) {
-        launch_colorfield(kc, sorted, n, ranges, sp, h_r, h2, hdr.particle_mass, psurf);
+        launch_colorfield(kc, sorted, n, ranges, skeys, sp, h_r, h2, hdr.particle_mass, psurf);
     } else {
         launch_surface_cells(kc, sp, occ, surf);
         if (yu13) launch_involved_cells(kc, sp, occ, surf, (uint8_t*)h->invol.ptr);
