@@ -130,6 +130,7 @@ def _load():
         "fsr_write_obj_indexed": (ctypes.c_int, [ctypes.c_char_p, c_vp, c_vp, c_u64, c_vp, c_u64]),
         "fsr_write_vis": (ctypes.c_int, [c_vp, ctypes.c_char_p, ctypes.c_char_p]),
         "fsr_check_division": (ctypes.c_int, [c_f32, P(c_u64), P(c_u64)]),
+        "fsr_check_spiky_grad": (ctypes.c_int, [ctypes.c_double, P(c_u64), P(c_u64)]),
         "fsr_write_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), c_vp, c_vp, c_u64]),
         "fsr_read_xyz_binary": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
     }

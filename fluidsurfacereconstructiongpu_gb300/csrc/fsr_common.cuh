@@ -165,6 +165,42 @@ __device__ __forceinline__ WarpBox warp_box(bool active, float x, float y, float
     return b;
 }
 
+// float(k * (double)x * (double)x) for k < 0 and x in (0, 1], the colour
+// field's spiky gradient as the reference evaluates it in double
+// (extractionOfSurfaceParticlesUsingColorField, cu:909-971), computed in
+// FP32 (this GPU's FP64 rate is a small fraction of its FP32 rate).  |k| is
+// split on the host into khi + klo (floats); |k| x^2 is formed as a float
+// pair with exact products (FMA) to within 2^-44 relative, and rounded to
+// float; the reference's value, within 2^-52 of the exact product, rounds to
+// the same float unless the exact product lies near a rounding midpoint.
+// Those cases (the pair's value within 2^-40 of a midpoint, about one
+// evaluation in 2^19) take the double expression itself.  fsr_check_spiky_grad
+// compares it with the double expression for every float x in (0, 1].
+// The double expression, out of line so that the compiler keeps it behind a
+// branch instead of evaluating it on every call.
+static __device__ __noinline__ float spiky_grad_double(float x, double k)
+{
+    return __double2float_rn(__dmul_rn(__dmul_rn(k, (double)x), (double)x));
+}
+
+__device__ __forceinline__ float spiky_grad(float x, float khi, float klo, double k)
+{
+    const float ph = __fmul_rn(khi, x);
+    const float pl = fmaf(khi, x, -ph);       // khi x = ph + pl exactly
+    const float b = fmaf(klo, x, pl);         // |k| x = ph + b (1 + 2^-46)
+    const float qh = __fmul_rn(ph, x);
+    const float ql = fmaf(ph, x, -qh);        // ph x = qh + ql exactly
+    const float l = fmaf(b, x, ql);           // |k| x^2 = qh + l (1 + 2^-45)
+    const float r = __fadd_rn(qh, l);
+    const float bb = __fsub_rn(r, qh);        // two-sum: err = qh + l - r exactly
+    const float err = __fadd_rn(__fsub_rn(qh, __fsub_rn(r, bb)), __fsub_rn(l, bb));
+    const float up = __fsub_rn(__int_as_float(__float_as_int(r) + 1), r);  // the ulps above and below r
+    const float dn = __fsub_rn(r, __int_as_float(__float_as_int(r) - 1));
+    const float margin = r * 0x1p-40f;
+    if (fmaf(0.5f, up, -err) <= margin || fmaf(0.5f, dn, err) <= margin) return spiky_grad_double(x, k);
+    return -r;
+}
+
 // a / b correctly rounded (the same float as __fdiv_rn(a, b)) for a >= 0,
 // b > 0, given rb = RN(1 / b) computed once on the host.  Markstein's
 // theorem (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,

@@ -190,8 +190,8 @@ __global__ void k_involved_cells(Grid sp, const uint8_t* __restrict__ occ, const
 __global__ void __launch_bounds__(kThreads) k_colorfield(const float4* __restrict__ sorted, uint32_t n,
                                                          const uint2* __restrict__ ranges,
                                                          const uint32_t* __restrict__ skeys, Grid sp, float h,
-                                                         float h_rcp, float h_lt2, double k_spiky, float mass,
-                                                         uint8_t* __restrict__ psurf)
+                                                         float h_rcp, float h_lt2, double k_spiky, float khi,
+                                                         float klo, float mass, uint8_t* __restrict__ psurf)
 {
     __shared__ float4 s_q[kThreads];    // staged candidates, per warp
     __shared__ float s_mr[kThreads];    // their m / rho
@@ -214,8 +214,8 @@ __global__ void __launch_bounds__(kThreads) k_colorfield(const float4* __restric
         // float is exact, so rounding it to float is the correctly rounded
         // FP32 difference (no FP64 work needed)
         const float x = __fsub_rn(1.0f, div_exact(d, h, h_rcp));
-        const double xd = (double)x;
-        const float grad = __double2float_rn(__dmul_rn(__dmul_rn(k_spiky, xd), xd));
+        // float(k x x) in double (cu:957); in FP32 when |k| is in range (khi > 0)
+        const float grad = khi > 0.f ? spiky_grad(x, khi, klo, k_spiky) : spiky_grad_double(x, k_spiky);
         const float inv = __fdiv_rn(1.0f, d);
         rx = __fmul_rn(rx, inv);
         ry = __fmul_rn(ry, inv);
@@ -902,8 +902,16 @@ void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, con
     if (!n) return;
     // -45 / (pi h^4) exactly as the reference evaluates it in double
     const double k = -45.0 / (3.1415926535 * (double)h2 * (double)h2);
+    // the FP32 form of the gradient needs |k| x^2 (x in (0, 1]) to stay a
+    // normal float: |k| within [1e-20, 1e30]; else the double expression
+    const double K = -k;
+    float khi = 0.f, klo = 0.f;
+    if (K >= 1e-20 && K <= 1e30) {
+        khi = (float)K;
+        klo = (float)(K - (double)khi);
+    }
     k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, skeys, sp, h, 1.0f / h,
-                                                           sqrt_threshold(h, false), k, mass, psurf);
+                                                           sqrt_threshold(h, false), k, khi, klo, mass, psurf);
     ++g_launches;
 }
 

@@ -28,7 +28,49 @@ __global__ void k_check_division(uint32_t hi_bits, float b, float rb, unsigned l
     if (local) atomicAdd(bad, local);
 }
 
+// Every float x in (0, 1]: spiky_grad must equal float(k x x) in double.
+__global__ void k_check_spiky(double k, float khi, float klo, unsigned long long* bad, unsigned long long* first_bad)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint32_t one = 0x3F800000u;
+    unsigned long long local = 0;
+    for (uint64_t i = 1 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= one; i += stride) {
+        const float x = __uint_as_float((uint32_t)i);
+        const float a = fsr::spiky_grad(x, khi, klo, k);
+        const float b = __double2float_rn(__dmul_rn(__dmul_rn(k, (double)x), (double)x));
+        if (__float_as_uint(a) != __float_as_uint(b)) {
+            ++local;
+            atomicMin(first_bad, (unsigned long long)i);
+        }
+    }
+    if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
+
+extern "C" fsr_status fsr_check_spiky_grad(double k, uint64_t* n_checked, uint64_t* n_mismatch)
+{
+    if (!(k < 0.0) || !(-k >= 1e-20 && -k <= 1e30) || !n_checked || !n_mismatch) return FSR_ERR_INVALID_ARGUMENT;
+    const float khi = (float)(-k), klo = (float)(-k - (double)khi);
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, 16) != cudaSuccess) return FSR_ERR_CUDA;
+    const unsigned long long init[2] = {0ull, ~0ull};
+    cudaError_t e = cudaMemcpy(d, init, 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        k_check_spiky<<<sms * 8, 256>>>(k, khi, klo, d, d + 1);
+        e = cudaGetLastError();
+    }
+    unsigned long long out[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, 16, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return FSR_ERR_CUDA;
+    *n_checked = 0x3F800000ull;
+    *n_mismatch = out[0];
+    return FSR_OK;
+}
 
 extern "C" fsr_status fsr_check_division(float b, uint64_t* n_checked, uint64_t* n_mismatch)
 {

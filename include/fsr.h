@@ -326,6 +326,12 @@ fsr_status fsr_batch_copy_mesh(const fsr_batch* b, uint32_t frame, float* pos, f
  * counts the results that differ (0 expected). */
 fsr_status fsr_check_division(float R, uint64_t* n_checked, uint64_t* n_mismatch);
 
+/* Self-check of the FP32 form of the colour field's gradient float(k x x)
+ * (evaluated in double by the reference; k < 0, |k| in [1e-20, 1e30]): runs
+ * it and the double expression for every float x in (0, 1] and counts the
+ * results that differ (0 expected). */
+fsr_status fsr_check_spiky_grad(double k, uint64_t* n_checked, uint64_t* n_mismatch);
+
 /* ---- file formats -------------------------------------------------- */
 
 /* Parses an .xyz file (data_format.txt; ReconstructorGPU.cpp:200-290).
