@@ -177,7 +177,8 @@ constexpr int kMoments = 35;             // moments of the unscaled kernel's pol
 // Per-warp shared memory of the forward kernel.
 struct WarpSlice {
     float4 rec[32 * 3];          // the current chunk's candidate records, one per lane
-    float4 vpos[kPassVerts];     // the pass's band vertices: position, band rank (bits)
+    uint32_t vloc[kPassVerts];   // the pass's band vertices: index in the group's box (vert_loc)
+    uint32_t vrank[kPassVerts];  // and band rank
     float4 box[2 * kPassTiles];  // per tile: lo, hi
     float psum[kPassTiles][32];  // per tile and lane: sum over the involved candidates
     float usum[kPassTiles][32];  // and over the non-involved ones
@@ -295,6 +296,21 @@ __device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r0.w;
 }
 
+// A listed vertex is kept as its index in the group's box, 10 bits per axis
+// (the box spans at most ratio + 1 <= 1001 vertices per axis); its position
+// is the scalar grid's vertex position (getVertexPos, FP32).
+__device__ __forceinline__ uint32_t vert_loc(int lx, int ly, int lz)
+{
+    return (uint32_t)lx | ((uint32_t)ly << 10) | ((uint32_t)lz << 20);
+}
+
+__device__ __forceinline__ float4 vert_pos(uint32_t loc, const int lo[3], const Grid& sc)
+{
+    return make_float4(vpos1(lo[0] + (int)(loc & 1023u), sc.min[0], sc.cs),
+                       vpos1(lo[1] + (int)((loc >> 10) & 1023u), sc.min[1], sc.cs),
+                       vpos1(lo[2] + (int)(loc >> 20), sc.min[2], sc.cs), 0.f);
+}
+
 // The layout of a pass of nv <= kPassVerts listed vertices: the pass's box
 // (pl, ph, on every lane), their order in 4 x 4 x 2-vertex bricks (tiles of
 // compact bricks instead of runs of rows: a smaller box per tile, fewer
@@ -302,14 +318,15 @@ __device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
 // is that of the atomics, which changes no result since a vertex's sum does
 // not depend on its tile and culling only skips exact zeros), and the box of
 // each 32-vertex tile.  hist: kPassVerts words of scratch.
-__device__ __forceinline__ void pass_layout(const float4* vpos, uint16_t* order, uint32_t* hist, float4* box,
-                                            uint32_t nv, float inv, int lane, float4& pl, float4& ph)
+__device__ __forceinline__ void pass_layout(const uint32_t* vloc, const int lo[3], const Grid& sc, uint16_t* order,
+                                            uint32_t* hist, float4* box, uint32_t nv, float inv, int lane, float4& pl,
+                                            float4& ph)
 {
     const uint32_t ntiles = (nv + 31) / 32;
     pl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f);
     ph = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
     for (uint32_t q = lane; q < nv; q += 32) {
-        const float4 v = vpos[q];
+        const float4 v = vert_pos(vloc[q], lo, sc);
         pl.x = fminf(pl.x, v.x); pl.y = fminf(pl.y, v.y); pl.z = fminf(pl.z, v.z);
         ph.x = fmaxf(ph.x, v.x); ph.y = fmaxf(ph.y, v.y); ph.z = fmaxf(ph.z, v.z);
     }
@@ -337,7 +354,7 @@ __device__ __forceinline__ void pass_layout(const float4* vpos, uint16_t* order,
             key[k] = 0;
             slot[k] = 0;
             if (q < nv) {
-                const float4 v = vpos[q];
+                const float4 v = vert_pos(vloc[q], lo, sc);
                 const int ix = __float2int_rn((v.x - pl.x) * inv) >> 2;
                 const int iy = __float2int_rn((v.y - pl.y) * inv) >> 2;
                 const int iz = __float2int_rn((v.z - pl.z) * inv) >> 1;
@@ -376,7 +393,7 @@ __device__ __forceinline__ void pass_layout(const float4* vpos, uint16_t* order,
     if ((uint32_t)lane < ntiles) {
         float4 tl = make_float4(3.0e38f, 3.0e38f, 3.0e38f, 0.f), th = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
         for (uint32_t q = 32 * lane; q < min(nv, 32 * lane + 32); ++q) {
-            const float4 v = vpos[order[q]];
+            const float4 v = vert_pos(vloc[order[q]], lo, sc);
             tl.x = fminf(tl.x, v.x); tl.y = fminf(tl.y, v.y); tl.z = fminf(tl.z, v.z);
             th.x = fmaxf(th.x, v.x); th.y = fmaxf(th.y, v.y); th.z = fmaxf(th.z, v.z);
         }
@@ -386,14 +403,15 @@ __device__ __forceinline__ void pass_layout(const float4* vpos, uint16_t* order,
     __syncwarp();
 }
 
-// The band vertices of a group's index box [lo, hi), listed into vpos as
-// (position, band rank) by row segments of at most 32 vertices (two bitset
+// The band vertices of a group's index box [lo, hi), listed into (vloc,
+// vrank) by row segments of at most 32 vertices (two bitset
 // words), `per` segments per step so that one step adds at most kPassVerts
 // vertices; pass(count) runs whenever the next step would not fit, and at
 // the end.
 template <class PassFn>
 __device__ __forceinline__ void list_band_vertices(const Grid& sc, const BandView& band, const int lo[3],
-                                                   const int hi[3], float4* vpos, int lane, PassFn&& pass)
+                                                   const int hi[3], uint32_t* vloc, uint32_t* vrank, int lane,
+                                                   PassFn&& pass)
 {
     const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
     const int nseg = (nx + 31) / 32;
@@ -434,8 +452,8 @@ __device__ __forceinline__ void list_band_vertices(const Grid& sc, const BandVie
             uint32_t slot = count + x - n;
             for (uint32_t m = rm; m; m &= m - 1u) {
                 const int bx = __ffs(m) - 1;
-                vpos[slot++] = make_float4(vpos1(x0 + bx, sc.min[0], sc.cs), vpos1(ry, sc.min[1], sc.cs),
-                                           vpos1(rz, sc.min[2], sc.cs), __uint_as_float(r0 + __popc(rm & ((1u << bx) - 1u))));
+                vloc[slot] = vert_loc(x0 + bx - lo[0], ry - lo[1], rz - lo[2]);
+                vrank[slot++] = r0 + __popc(rm & ((1u << bx) - 1u));
             }
             count += tot;
         }
@@ -523,7 +541,7 @@ __device__ __forceinline__ float unscaled_sum(const float* m, float zx, float zy
 // tile the warp keeps the candidates whose support sphere reaches the
 // tile's box and each lane adds their terms for its vertex of that tile.
 // A vertex's sum takes the candidates in window order.
-__global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32_t ratio, Counters* ctr)
+__global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uint32_t ratio, Counters* ctr)
 {
     __shared__ WarpSlice slices[kFWarps];
     const int lane = threadIdx.x & 31;
@@ -580,8 +598,8 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             const uint32_t ntiles = (nv + 31) / 32;
             // the pass's box, brick order and tile boxes
             float4 pl, ph;
-            pass_layout(w.vpos, w.order, reinterpret_cast<uint32_t*>(&w.psum[0][0]), w.box, nv, 1.0f / a.sc.cs, lane,
-                        pl, ph);  // psum is zeroed below
+            pass_layout(w.vloc, lo, a.sc, w.order, reinterpret_cast<uint32_t*>(&w.psum[0][0]), w.box, nv,
+                        1.0f / a.sc.cs, lane, pl, ph);  // psum is zeroed below
             // two sums per vertex: the involved particles' terms, then the
             // non-involved particles' (the unscaled kernel: about 1e-7 each,
             // thousands of them), added among themselves and joined at the
@@ -620,7 +638,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                             const uint32_t m = __ballot_sync(0xffffffffu, keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]));
                             const uint32_t v = 32 * t + lane;
                             if (m && v < nv) {
-                                const float4 vp = w.vpos[w.order[v]];
+                                const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
                                 float s = w.psum[t][lane];
                                 // two kept candidates per step, evaluated without
                                 // branches; their terms enter the sum in order
@@ -657,7 +675,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 for (int t = 0; t < kPassTiles; ++t) {
                     const uint32_t v = 32 * t + lane;
                     if ((uint32_t)t < ntiles && v < nv) {
-                        const float4 vp = w.vpos[w.order[v]];
+                        const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
                         w.usum[t][lane] = unscaled_sum(w.mom, vp.x - ox, vp.y - oy, vp.z - oz);
                     }
                 }
@@ -676,7 +694,7 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
                 for (int t = 0; t < kPassTiles; ++t) {
                     const uint32_t v = 32 * t + lane;
                     if ((uint32_t)t < ntiles && v < nv) {
-                        const float4 vp = w.vpos[w.order[v]];
+                        const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
                         float su = w.usum[t][lane];
                         uint32_t k = 0;
                         for (; k + 2 <= cnt; k += 2) {
@@ -705,14 +723,14 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
             for (int t = 0; t < kPassTiles; ++t) {
                 const uint32_t v = 32 * t + lane;
                 if (v < nv) {
-                    const uint32_t rank = __float_as_uint(w.vpos[w.order[v]].w);
+                    const uint32_t rank = w.vrank[w.order[v]];
                     if (rank < nb) a.phi[rank] = (w.psum[t][lane] + w.usum[t][lane]) - 0.5f;
                 }
             }
             __syncwarp();
         };
 
-        list_band_vertices(a.sc, a.band, lo, hi, w.vpos, lane, pass);
+        list_band_vertices(a.sc, a.band, lo, hi, w.vloc, w.vrank, lane, pass);
         __syncwarp();
     }
 }
@@ -728,7 +746,8 @@ __global__ void __launch_bounds__(kFT) k_field_aniso_grouped(GroupArgs a, uint32
 // walk narrows away lie beyond h and add nothing.
 struct IsoSlice {
     float4 rec[32];                // the current chunk's candidates, one per lane
-    float4 vpos[kPassVerts];       // the pass's band vertices: position, band rank (bits)
+    uint32_t vloc[kPassVerts];     // the pass's band vertices: index in the group's box (vert_loc)
+    uint32_t vrank[kPassVerts];    // and band rank
     float4 box[2 * kPassTiles];    // per tile: lo, hi
     float sum[4][kPassTiles][32];  // per vertex: weight sum, then (ZB05) sum w (x - v)
     uint16_t order[kPassVerts];    // the pass's vertices in brick order
@@ -796,8 +815,8 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
 
         auto pass = [&](uint32_t nv) {
             float4 pl, ph;
-            pass_layout(w.vpos, w.order, reinterpret_cast<uint32_t*>(&w.sum[0][0][0]), w.box, nv, 1.0f / a.sc.cs, lane,
-                        pl, ph);  // the sums are zeroed next
+            pass_layout(w.vloc, lo, a.sc, w.order, reinterpret_cast<uint32_t*>(&w.sum[0][0][0]), w.box, nv,
+                        1.0f / a.sc.cs, lane, pl, ph);  // the sums are zeroed next
             const uint32_t ntiles = (nv + 31) / 32;
             for (int k = 0; k < kSums; ++k)
                 for (int t = 0; t < kPassTiles; ++t) w.sum[k][t][lane] = 0.f;
@@ -822,7 +841,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                         const uint32_t m = __ballot_sync(0xffffffffu, keep && within(q, w.box[2 * t], w.box[2 * t + 1], cr2));
                         const uint32_t v = 32 * t + lane;
                         if (m && v < nv) {
-                            const float4 vp = w.vpos[w.order[v]];
+                            const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
                             float ws = w.sum[0][t][lane];
                             float ax = 0.f, ay = 0.f, az = 0.f;
                             if (!TC01) {
@@ -862,7 +881,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
             for (int t = 0; t < (int)ntiles; ++t) {
                 const uint32_t v = 32 * t + lane;
                 if (v < nv) {
-                    const uint32_t rank = __float_as_uint(w.vpos[w.order[v]].w);
+                    const uint32_t rank = w.vrank[w.order[v]];
                     if (rank < nb) {
                         const float ws = w.sum[0][t][lane];
                         if (TC01) {
@@ -882,7 +901,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
             }
             __syncwarp();
         };
-        list_band_vertices(a.sc, band, lo, hi, w.vpos, lane, pass);
+        list_band_vertices(a.sc, band, lo, hi, w.vloc, w.vrank, lane, pass);
         __syncwarp();
     }
 }

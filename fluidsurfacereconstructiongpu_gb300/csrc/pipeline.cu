@@ -111,7 +111,9 @@ fsr_status cuda_fail(fsr_handle* h, cudaError_t e, const char* where)
 bool valid_params(const fsr_params& p)
 {
     if (p.method > FSR_METHOD_AKINCI12) return false;
-    if (p.grid_ratio == 0 || !(p.cell_size_scale > 0.0f) || !std::isfinite(p.iso_value)) return false;
+    // the field kernels index a group's vertex box with 10 bits per axis (ratio + 1 vertices)
+    if (p.grid_ratio == 0 || p.grid_ratio > 1000 || !(p.cell_size_scale > 0.0f) || !std::isfinite(p.iso_value))
+        return false;
     if (p.method == FSR_METHOD_YU13 && !(p.aniso_radius_over_h > 0.0f)) return false;
     return true;
 }

@@ -55,7 +55,7 @@ typedef enum fsr_method {
 typedef struct fsr_params {
     uint32_t method;             /* fsr_method */
     float iso_value;             /* SimParam.isoValue */
-    uint32_t grid_ratio;         /* SimParam.scSpGridResRatio: spatial cell / scalar cell */
+    uint32_t grid_ratio;         /* SimParam.scSpGridResRatio: spatial cell / scalar cell (1..1000) */
     float cell_size_scale;       /* SimParam.spatialCellSizeScale: spatial cell / h */
     float smoothing_lambda;      /* SimParam.lambdaForSmoothed (Yu13) */
     float aniso_radius_over_h;   /* SimParam.anisotropicRadius / h (Yu13: 2) */
