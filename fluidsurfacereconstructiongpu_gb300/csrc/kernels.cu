@@ -745,12 +745,17 @@ __device__ __forceinline__ void normalize_guarded(float n[3])
 // generateTriangles (cu:383-463), or with host_mc the host marching cubes
 // of Akinci12 (MarchingCubesCPU.cpp:3-72: no normal sign flip, guarded
 // normalisation, epsilon test in double).
-__global__ void k_mc_generate(McArgs a, const Counters* ctr)
+__global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counters* ctr)
 {
+    // corner values and normals per thread in shared memory ([corner][thread]),
+    // so that the cut edges can index them without spilling registers
+    __shared__ float s_val[8 * kThreads];
+    __shared__ float s_nrm[24 * kThreads];
     const uint32_t nq = min(ctr->n_valid, a.cap_valid);
     const uint32_t ntot = ctr->n_mesh_verts;
     if (ntot > a.cap_mesh) return;
     const float sgn = a.host_mc ? 1.0f : (a.iso < 0.0f ? -1.0f : 1.0f);
+    const int tid = threadIdx.x;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
         const uint32_t t = a.valid[q];
         const uint32_t info = a.mc[t];
@@ -759,63 +764,50 @@ __global__ void k_mc_generate(McArgs a, const Counters* ctr)
         const uint32_t base = a.vofs[t];
         uint32_t x, y, z;
         unlin3(a.sv[t], a.sc, x, y, z);
-        float val[8], cp[8][3], cn[8][3];
-#pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int cx = (int)x + mc::cornerDx(i), cy = (int)y + mc::cornerDy(i),
-                      cz = (int)z + mc::cornerDz(i);
-            val[i] = field_at(a, cx, cy, cz);
-            cp[i][0] = vpos1(cx, a.sc.min[0], a.sc.cs);
-            cp[i][1] = vpos1(cy, a.sc.min[1], a.sc.cs);
-            cp[i][2] = vpos1(cz, a.sc.min[2], a.sc.cs);
-            cn[i][0] = field_at(a, cx - 1, cy, cz) - field_at(a, cx + 1, cy, cz);
-            cn[i][1] = field_at(a, cx, cy - 1, cz) - field_at(a, cx, cy + 1, cz);
-            cn[i][2] = field_at(a, cx, cy, cz - 1) - field_at(a, cx, cy, cz + 1);
-            if (a.host_mc) normalize_guarded(cn[i]);
-            else normalize_fast(cn[i]);
-        }
-        const uint32_t ef = c_mc.eflags[cs];
-        float ip[12][3], in[12][3];
-#pragma unroll
-        for (int e = 0; e < 12; ++e) {
-            if (!(ef & (1u << e))) continue;
-            const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
-            const float d = val[i1] - val[i0];
-            const float f = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - val[i0]) / d;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                ip[e][k] = fmaf(f, cp[i1][k] - cp[i0][k], cp[i0][k]);
-                in[e][k] = fmaf(f, cn[i1][k] - cn[i0][k], cn[i0][k]);
-            }
-            if (a.host_mc) normalize_guarded(in[e]);
-            else normalize_fast(in[e]);
+            const int cx = (int)x + mc::cornerDx(i), cy = (int)y + mc::cornerDy(i), cz = (int)z + mc::cornerDz(i);
+            s_val[i * kThreads + tid] = field_at(a, cx, cy, cz);
+            float cn[3] = {field_at(a, cx - 1, cy, cz) - field_at(a, cx + 1, cy, cz),
+                           field_at(a, cx, cy - 1, cz) - field_at(a, cx, cy + 1, cz),
+                           field_at(a, cx, cy, cz - 1) - field_at(a, cx, cy, cz + 1)};
+            if (a.host_mc) normalize_guarded(cn);
+            else normalize_fast(cn);
+            s_nrm[(3 * i) * kThreads + tid] = cn[0];
+            s_nrm[(3 * i + 1) * kThreads + tid] = cn[1];
+            s_nrm[(3 * i + 2) * kThreads + tid] = cn[2];
         }
         const uint64_t tri = c_mc.tri[cs];
         for (uint32_t k = 0; k < nv; ++k) {
             const int e = (int)((tri >> (4u * k)) & 0xFu);
-            const uint64_t o = 3ull * (base + k);
-            float px = 0.f, py = 0.f, pz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+            const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
+            const float v0 = s_val[i0 * kThreads + tid], v1 = s_val[i1 * kThreads + tid];
+            const float d = v1 - v0;
+            const float f = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - v0) / d;
+            const int c0[3] = {(int)x + mc::cornerDx(i0), (int)y + mc::cornerDy(i0), (int)z + mc::cornerDz(i0)};
+            const int c1[3] = {(int)x + mc::cornerDx(i1), (int)y + mc::cornerDy(i1), (int)z + mc::cornerDz(i1)};
+            float ip[3], in[3];
 #pragma unroll
-            for (int ee = 0; ee < 12; ++ee)
-                if (ee == e) {
-                    px = ip[ee][0]; py = ip[ee][1]; pz = ip[ee][2];
-                    nx = in[ee][0]; ny = in[ee][1]; nz = in[ee][2];
-                }
-            a.out_pos[o] = px;
-            a.out_pos[o + 1] = py;
-            a.out_pos[o + 2] = pz;
-            a.out_nrm[o] = sgn * nx;
-            a.out_nrm[o + 1] = sgn * ny;
-            a.out_nrm[o + 2] = sgn * nz;
+            for (int kk = 0; kk < 3; ++kk) {
+                const float p0 = vpos1(c0[kk], a.sc.min[kk], a.sc.cs), p1 = vpos1(c1[kk], a.sc.min[kk], a.sc.cs);
+                ip[kk] = fmaf(f, p1 - p0, p0);
+                const float n0 = s_nrm[(3 * i0 + kk) * kThreads + tid], n1 = s_nrm[(3 * i1 + kk) * kThreads + tid];
+                in[kk] = fmaf(f, n1 - n0, n0);
+            }
+            if (a.host_mc) normalize_guarded(in);
+            else normalize_fast(in);
+            const uint64_t o = 3ull * (base + k);
+            a.out_pos[o] = ip[0];
+            a.out_pos[o + 1] = ip[1];
+            a.out_pos[o + 2] = ip[2];
+            a.out_nrm[o] = sgn * in[0];
+            a.out_nrm[o + 1] = sgn * in[1];
+            a.out_nrm[o + 2] = sgn * in[2];
             if (a.out_key) {
                 // the edge's lower end point and its axis (the one coordinate
                 // in which the two corners differ)
-                const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
-                const uint32_t lx = x + (uint32_t)min(mc::cornerDx(i0), mc::cornerDx(i1));
-                const uint32_t ly = y + (uint32_t)min(mc::cornerDy(i0), mc::cornerDy(i1));
-                const uint32_t lz = z + (uint32_t)min(mc::cornerDz(i0), mc::cornerDz(i1));
-                const uint32_t axis = mc::cornerDx(i0) != mc::cornerDx(i1) ? 0u
-                                      : (mc::cornerDy(i0) != mc::cornerDy(i1) ? 1u : 2u);
+                const uint32_t lx = (uint32_t)min(c0[0], c1[0]), ly = (uint32_t)min(c0[1], c1[1]),
+                               lz = (uint32_t)min(c0[2], c1[2]);
+                const uint32_t axis = c0[0] != c1[0] ? 0u : (c0[1] != c1[1] ? 1u : 2u);
                 const uint64_t lin = (uint64_t)lx + (uint64_t)a.sc.res[0] * ((uint64_t)ly + (uint64_t)a.sc.res[1] * lz);
                 a.out_key[base + k] = 3ull * lin + axis;
             }
