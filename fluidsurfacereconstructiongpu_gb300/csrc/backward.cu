@@ -479,7 +479,7 @@ __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool 
     }
 }
 
-__global__ void k_cov_backward(BwdArgs a, CovArgs f)
+__global__ void __launch_bounds__(kT, 3) k_cov_backward(BwdArgs a, CovArgs f)
 {
     __shared__ float4 s_q[kT];  // 32 staged particles per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
