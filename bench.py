@@ -105,7 +105,8 @@ class ClockSampler:
 
     def __init__(self, gpu_index):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), f"fsr_clocks_{os.getpid()}.csv")
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")

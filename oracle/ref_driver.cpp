@@ -15,7 +15,7 @@
  * 1450-1456: 256-thread blocks).  Logical threads run in an OpenMP loop with
  * the launch coordinates set per OS thread.
  *
- * Two deliberate deviations, both documented in the design doc:
+ * Two deliberate deviations:
  *  - the smoothing kernel (ReconstructionCUDA.cu:609, bound "threadId >
  *    size") is run over exactly N threads, so the out-of-bounds thread N
  *    never executes;
