@@ -10,7 +10,9 @@ reference's parameters; loss = mean over mesh vertices of (|v - c| - 0.32)^2.
          whole pipeline for the same particles; one JSON line per particle is
          appended to ROWS.jsonl, and a rerun skips the particles already there;
          hours of CPU time)
-  python tests/golden/fd_sphere262k.py summary ROWS.jsonl SUMMARY.json
+  python tests/golden/fd_sphere262k.py summary ROWS.jsonl SUMMARY.json [GRAD.npz]
+        (GRAD.npz: a later gradient of the same particles replaces the one
+         recorded in the rows)
 
 The fd step skips coordinates whose perturbation changes a discrete decision
 (sort order, surface flags, band, cubes, cases, involved cells) or where the
@@ -123,7 +125,13 @@ def run_fd(inp, rows_path):
         print(f"{n_done + 1}/{len(d['idx'])} particles, {time.time() - t0:.0f} s", flush=True)
 
 
-def run_summary(rows_path, out):
+def run_summary(rows_path, out, grad_path=None):
+    # the rows carry the gradient the fd step was started with; a later
+    # gradient file (the same particles) replaces it
+    override = None
+    if grad_path:
+        g = np.load(grad_path)
+        override = {int(i): gi for i, gi in zip(g["idx"], g["grad"])}
     rows, skipped_structure, skipped_kink, n_particles = [], 0, 0, 0
     for line in open(rows_path):
         if not line.strip():
@@ -136,7 +144,8 @@ def run_summary(rows_path, out):
             elif c.get("skip") == "kink":
                 skipped_kink += 1
             else:
-                rows.append((rec["particle"], c["axis"], c["grad"], c["fd"]))
+                gval = float(override[rec["particle"]][c["axis"]]) if override is not None else c["grad"]
+                rows.append((rec["particle"], c["axis"], gval, c["fd"]))
     r = np.array(rows)
     scale = float(np.abs(r[:, 3]).max()) if len(r) else 0.0
     err = np.abs(r[:, 2] - r[:, 3]) if len(r) else np.zeros(0)
@@ -145,6 +154,7 @@ def run_summary(rows_path, out):
         "workload": "sphere_ball(262144, radius 0.3, seed 4): 262,144 particles, anisotropic field, reference parameters",
         "loss": "mean over mesh vertices of (|v - (0.5,0.5,0.5)| - 0.32)^2",
         "fd": "FP64 oracle, central differences, delta = 1e-4 r",
+        "gradient": os.path.basename(grad_path) if grad_path else "as recorded in the rows",
         "particles": n_particles, "coordinates": 3 * n_particles, "compared": int(len(r)),
         "skipped_structure_change": skipped_structure, "skipped_kink": skipped_kink,
         "nonzero_fd": int(nz.sum()), "max_abs_fd": scale,
@@ -163,4 +173,4 @@ if __name__ == "__main__":
     elif sys.argv[1] == "fd":
         run_fd(sys.argv[2], sys.argv[3])
     else:
-        run_summary(sys.argv[2], sys.argv[3])
+        run_summary(sys.argv[2], sys.argv[3], sys.argv[4] if len(sys.argv) > 4 else None)
