@@ -331,12 +331,14 @@ __global__ void __launch_bounds__(kThreads) k_colorfield(const float4* __restric
 // estimationOfSurfaceVertices (cu:554-595): vertices in the clamped box
 // idx-3 .. idx+3 (x upper bound exclusive) within 1.5h of a surface
 // particle.  `thr` is the largest float whose double value is below
-// 1.5*h, so dist <= thr reproduces the reference's double comparison.
+// 1.5*h, so dist <= thr reproduces the reference's double comparison; the
+// kernel tests the squared distance against thr2 = sqrt_threshold(thr,
+// true), the same decision without the square root.
 // Each (y,z) row of at most 6 vertices is OR-ed into the bitset with at most
 // two atomics.
 __global__ void k_band_stamp(const float4* __restrict__ sorted, const uint32_t* __restrict__ skeys,
                              const uint8_t* __restrict__ surf, const uint8_t* __restrict__ psurf, uint32_t n,
-                             Grid sc, float thr, uint32_t* __restrict__ bits, Counters* ctr)
+                             Grid sc, float thr2, uint32_t* __restrict__ bits, Counters* ctr)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     bool is_s = false;
@@ -356,8 +358,8 @@ __global__ void k_band_stamp(const float4* __restrict__ sorted, const uint32_t* 
             uint32_t m0 = 0, m1 = 0;
             for (int x = w.lo[0]; x < w.hi[0]; ++x) {
                 const float dx = __fsub_rn(vpos1(x, sc.min[0], sc.cs), p.x);
-                const float dist = __fsqrt_rn(dot3_rn(dx, dy, dz));
-                if (dist <= thr) {
+                // sqrt_rn(d2) <= thr  <=>  d2 < thr2 (the smallest float whose root exceeds thr)
+                if (dot3_rn(dx, dy, dz) < thr2) {
                     const uint32_t v = v0 + (uint32_t)(x - w.lo[0]);
                     if ((v >> 5) == word0) m0 |= 1u << (v & 31u);
                     else m1 |= 1u << (v & 31u);
@@ -912,7 +914,8 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
                        Counters* ctr)
 {
     if (!n) return;
-    k_band_stamp<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc, thr, bits, ctr);
+    k_band_stamp<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc,
+                                                           sqrt_threshold(thr, true), bits, ctr);
     ++g_launches;
 }
 
