@@ -242,3 +242,20 @@ def test_same_bytes_as_the_stream_code(tmp_path):
     api.write_obj(a, api.Mesh(positions=pos, normals=nrm))
     port.io_port_write_obj(b.encode(), pos.ctypes.data, nrm.ctypes.data, nv)
     assert open(a, "rb").read() == open(b, "rb").read()
+
+
+def test_indexed_obj_writer(tmp_path):
+    """Host-only: the indexed .obj layout, and out-of-range indices rejected."""
+    from fluidsurfacereconstructiongpu_gb300 import api, _native
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    nrm = np.ones((4, 3), np.float32)
+    tri = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    out = tmp_path / "w.obj"
+    api.write_obj(str(out), api.IndexedMesh(pos, nrm, tri))
+    lines = out.read_text().splitlines()
+    assert lines[:4] == ["v 0 0 0", "v 1 0 0", "v 0 1 0", "v 0 0 1"]
+    assert lines[4:8] == ["vn 1 1 1"] * 4
+    assert lines[8:] == ["f 1//1 2//2 3//3 ", "f 1//1 3//3 4//4 "]
+    with pytest.raises(_native.FsrError) as e:
+        api.write_obj(str(out), api.IndexedMesh(pos, nrm, np.array([[0, 1, 4]], np.uint32)))
+    assert e.value.status == 1
