@@ -190,7 +190,29 @@ struct WarpSlice {
     uint32_t cinv[128];
     uint32_t ncells;             // entries of the candidate tables
     uint32_t total_inv;          // candidates of involved cells (they come first)
+    uint32_t ninv_cells;         // and the number of those cells
 };
+
+// The window cells of candidates cb .. cb + 31 of a sweep through the
+// tables, one per lane, from the table boundaries that fall inside the
+// chunk (one shared load and a warp OR instead of a binary search per
+// lane).  k0 is a cell with cpre[k0] <= cb < cpre[k0 + 1] on entry (the
+// sweep's first cell, or the value the previous chunk left) and is advanced
+// to the cell of cb + 31.  Every lane calls it; the cell of a lane whose
+// candidate lies at or beyond the sweep's end is not used.
+__device__ __forceinline__ int chunk_cell(uint32_t cb, int lane, const uint32_t* cpre, uint32_t ncells, uint32_t& k0)
+{
+    const uint32_t k = k0 + 1u + (uint32_t)lane;
+    uint32_t bit = 0;
+    if (k <= ncells) {
+        const uint32_t d = cpre[k] - cb;  // cpre[k] >= cpre[k0 + 1] > cb
+        if (d < 32u) bit = 1u << d;
+    }
+    const uint32_t bm = __reduce_or_sync(0xffffffffu, bit);
+    const int cell = (int)(k0 + (uint32_t)__popc(bm & (0xffffffffu >> (31 - lane))));
+    k0 += (uint32_t)__popc(bm);
+    return cell;
+}
 
 // Warp-level version of group_candidates: the same cells, listed with the
 // involved cells first and the other non-empty cells after them (each part
@@ -261,7 +283,10 @@ __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ra
             slot += __popc(m);
             running += __shfl_sync(0xffffffffu, x, 31);
         }
-        if (part == 0 && lane == 0) w.total_inv = running;
+        if (part == 0 && lane == 0) {
+            w.total_inv = running;
+            w.ninv_cells = slot;
+        }
     }
     if (lane == 0) {
         w.cpre[slot] = running;
@@ -546,7 +571,6 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
     __shared__ WarpSlice slices[kFWarps];
     const int lane = threadIdx.x & 31;
     WarpSlice& w = slices[threadIdx.x >> 5];
-    const CandTables tabs{w.cstart, w.cpre, w.cinv};
     const uint32_t nb = min(ctr->n_band, a.cap);
     const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
 
@@ -574,6 +598,7 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                 MomAcc acc;
                 acc.zero();
                 float y2max = 0.f;
+                const CandTables tabs{w.cstart, w.cpre, w.cinv};
                 for (uint32_t j = w.total_inv + lane; j < total; j += 32) {
                     int cell;
                     const uint32_t i = candidate(j, tabs, &cell, (int)w.ncells);
@@ -609,16 +634,17 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
             // need not be unrolled (the kernel's code stays small enough for
             // the instruction cache)
             for (int t = 0; t < kPassTiles; ++t) w.psum[t][lane] = w.usum[t][lane] = 0.f;
-            const uint32_t ncells = w.ncells, total_inv = w.total_inv;
+            const uint32_t total_inv = w.total_inv;
             // involved candidates: staged with their G, culled per tile by
             // their support sphere, evaluated two at a time
+            uint32_t k0 = 0;
             for (uint32_t cb = 0; cb < total_inv; cb += 32) {
                 const uint32_t j = cb + lane;
                 bool keep = false;
                 float4 r0 = make_float4(0.f, 0.f, 0.f, -1.f);
+                const int cell = chunk_cell(cb, lane, w.cpre, w.ncells, k0);
                 if (j < total_inv) {
-                    int cell;
-                    const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
+                    const uint32_t i = w.cstart[cell] + (j - w.cpre[cell]);
                     const float4* qsrc = a.qrec + 3ull * i;
                     r0 = __ldg(qsrc);
                     keep = reaches(r0, pl, ph);
@@ -680,11 +706,12 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                     }
                 }
             }
+            k0 = w.ninv_cells;
             for (uint32_t cb = use_mom ? total : total_inv; cb < total; cb += 32) {
                 const uint32_t j = cb + lane;
+                const int cell = chunk_cell(cb, lane, w.cpre, w.ncells, k0);
                 if (j < total) {
-                    int cell;
-                    const uint32_t i = candidate(j, tabs, &cell, (int)ncells);
+                    const uint32_t i = w.cstart[cell] + (j - w.cpre[cell]);
                     const float4 sm = __ldg(&a.smoothed[i]);
                     w.rec[lane] = make_float4(sm.x, sm.y, sm.z, a.sigma * sm.w);
                 }
