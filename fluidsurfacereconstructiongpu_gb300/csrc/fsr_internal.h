@@ -72,7 +72,7 @@ struct fsr_handle {
     // vertex-sized
     fsr::DevBuf bits, prefix, scan_tmp;
     // band-sized
-    fsr::DevBuf sv, phi, mc, vofs, qpos, valid;
+    fsr::DevBuf sv, phi, mc, vofs, valid;
     // mesh
     fsr::DevBuf mesh_pos, mesh_nrm;
     // vertex welding (FSR_FLAG_WELD)

@@ -1,6 +1,7 @@
 // Per-frame kernels of the reconstruction path.  Each kernel names the
 // reference kernel it replaces (ReconstructionCUDA.cu, "cu").
 #include "kernels.h"
+#include "primitives.h"
 #include "cov_solver.cuh"
 
 #include <algorithm>
@@ -703,24 +704,126 @@ __global__ void k_mc_classify(McArgs a, const Counters* ctr)
     }
 }
 
-__global__ void k_valid_list(McArgs a, Counters* ctr)
+// The marching-cubes offsets in one reduce-then-scan over the classify
+// words (generateTriangles' vertex offsets and compactValidSurfaceCubes:
+// cu:367-380 with the scans of cu:1154-1172).  Per band position t: vofs[t]
+// = the vertices of the cubes before t, and a cube with vertices is listed
+// at valid[its rank among such cubes] = t.  Within a 4096-position tile both
+// counts fit 16 bits (at most 15 x 4096 vertices), so each element is one
+// word, vertices low and cubes high, and the block scans add such words;
+// the tile totals are kept apart, as full words.
+__device__ __forceinline__ uint32_t mc_pair(uint32_t info)
 {
-    const uint32_t nb = min(ctr->n_band, a.cap_band);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (ctr->n_valid > a.cap_valid) {
-            atomicOr(&ctr->overflow, 2u);
-            atomicMax(&ctr->need_valid, ctr->n_valid);
+    const uint32_t nv = info & 0xFFu;
+    return nv | (nv != 0u ? 0x10000u : 0u);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_mc_tile_reduce(McArgs a, const Counters* ctr, uint32_t* tile_sums,
+                                                                 uint32_t ntiles_max)
+{
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    const uint32_t n = min(ctr->n_band, a.cap_band);
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t base = (uint64_t)tile * kScanTile;
+        uint32_t s = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint64_t i = base + k * kScanThreads + threadIdx.x;
+            if (i < n) s += mc_pair(__ldg(a.mc + i));
         }
-        if (ctr->n_mesh_verts > a.cap_mesh) {
+        const uint32_t incl = block_inclusive_scan(s, warp_sums);
+        if (threadIdx.x == kScanThreads - 1) {
+            tile_sums[tile] = incl & 0xFFFFu;
+            tile_sums[ntiles_max + tile] = incl >> 16;
+        }
+        __syncthreads();
+    }
+}
+
+// One block: exclusive scans of both tile totals in place; the frame's
+// vertex and cube counts, and the pool overflow flags.
+__global__ void __launch_bounds__(kScanThreads) k_mc_scan_tile_sums(McArgs a, Counters* ctr, uint32_t* tile_sums,
+                                                                    uint32_t ntiles_max)
+{
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    __shared__ uint32_t last[2];
+    const uint32_t n = min(ctr->n_band, a.cap_band);
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
+    uint32_t carry[2] = {0u, 0u};
+    for (uint32_t b = 0; b < ntiles; b += kScanThreads) {
+        const uint32_t i = b + threadIdx.x;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            uint32_t* ts = tile_sums + h * ntiles_max;
+            const uint32_t x = i < ntiles ? ts[i] : 0u;
+            const uint32_t incl = block_inclusive_scan(x, warp_sums);
+            if (i < ntiles) ts[i] = carry[h] + incl - x;
+            if (threadIdx.x == kScanThreads - 1) last[h] = incl;
+            __syncthreads();
+            carry[h] += last[h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        ctr->n_mesh_verts = carry[0];
+        ctr->n_valid = carry[1];
+        if (carry[1] > a.cap_valid) {
+            atomicOr(&ctr->overflow, 2u);
+            atomicMax(&ctr->need_valid, carry[1]);
+        }
+        if (carry[0] > a.cap_mesh) {
             atomicOr(&ctr->overflow, 4u);
-            atomicMax(&ctr->need_mesh, ctr->n_mesh_verts);
+            atomicMax(&ctr->need_mesh, carry[0]);
         }
     }
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x) {
-        if ((a.mc[t] & 0xFFu) != 0u) {
-            const uint32_t q = a.qpos[t];
-            if (q < a.cap_valid) a.valid[q] = t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_mc_tile_scan(McArgs a, const Counters* ctr,
+                                                               const uint32_t* tile_prefix, uint32_t ntiles_max)
+{
+    __shared__ uint32_t warp_sums[kScanThreads / 32];
+    __shared__ uint32_t tile_vals[kScanTile];
+    const uint32_t n = min(ctr->n_band, a.cap_band);
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
+    for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t base = (uint64_t)tile * kScanTile;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t j = k * kScanThreads + threadIdx.x;
+            const uint64_t i = base + j;
+            tile_vals[j] = i < n ? mc_pair(__ldg(a.mc + i)) : 0u;
         }
+        __syncthreads();
+        // each thread owns kScanItems consecutive positions
+        uint32_t local[kScanItems];
+        uint32_t s = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            local[k] = tile_vals[threadIdx.x * kScanItems + k];
+            s += local[k];
+        }
+        const uint32_t incl = block_inclusive_scan(s, warp_sums);
+        uint32_t run = incl - s;  // packed exclusive prefix within the tile
+        const uint32_t pv = tile_prefix[tile], pq = tile_prefix[ntiles_max + tile];
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint64_t t = base + threadIdx.x * kScanItems + k;
+            if (local[k] != 0u && t < n) {
+                const uint32_t q = pq + (run >> 16);
+                if (q < a.cap_valid) a.valid[q] = (uint32_t)t;
+            }
+            tile_vals[threadIdx.x * kScanItems + k] = pv + (run & 0xFFFFu);
+            run += local[k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t j = k * kScanThreads + threadIdx.x;
+            const uint64_t i = base + j;
+            if (i < n) a.vofs[i] = tile_vals[j];
+        }
+        __syncthreads();
     }
 }
 
@@ -959,10 +1062,19 @@ void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr)
     ++g_launches;
 }
 
-void launch_valid_list(const KernelCtx& c, const McArgs& a, Counters* ctr)
+size_t mc_offsets_scratch_words(uint32_t cap_band)
 {
-    k_valid_list<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
-    ++g_launches;
+    return 2 * (size_t)((cap_band + kScanTile - 1) / kScanTile) + 2;
+}
+
+void launch_mc_offsets(const KernelCtx& c, const McArgs& a, Counters* ctr, uint32_t* scratch)
+{
+    const uint32_t ntiles_max = (a.cap_band + kScanTile - 1) / kScanTile;
+    const uint32_t g = std::max<uint32_t>(1, std::min<uint32_t>(ntiles_max, 65535));
+    k_mc_tile_reduce<<<g, kScanThreads, 0, c.stream>>>(a, ctr, scratch, ntiles_max);
+    k_mc_scan_tile_sums<<<1, kScanThreads, 0, c.stream>>>(a, ctr, scratch, ntiles_max);
+    k_mc_tile_scan<<<g, kScanThreads, 0, c.stream>>>(a, ctr, scratch, ntiles_max);
+    g_launches += 3;
 }
 
 void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr)

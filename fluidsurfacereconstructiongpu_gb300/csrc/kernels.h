@@ -142,8 +142,7 @@ struct McArgs {
     BandView band;
     const uint32_t* sv;
     uint32_t* mc;          // per band vertex: nverts | case << 8
-    const uint32_t* vofs;  // exclusive scan of nverts
-    const uint32_t* qpos;  // exclusive scan of (nverts != 0)
+    uint32_t* vofs;        // exclusive scan of nverts
     uint32_t* valid;       // valid cube list (positions in sv)
     float* out_pos;
     float* out_nrm;
@@ -153,7 +152,10 @@ struct McArgs {
     uint32_t cap_band, cap_valid, cap_mesh;
 };
 void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr);
-void launch_valid_list(const KernelCtx& c, const McArgs& a, Counters* ctr);
+// vofs, the valid cube list and the vertex / cube counts from the classify
+// words (3 launches); scratch: mc_offsets_scratch_words(cap_band) words
+size_t mc_offsets_scratch_words(uint32_t cap_band);
+void launch_mc_offsets(const KernelCtx& c, const McArgs& a, Counters* ctr, uint32_t* scratch);
 void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr);
 
 // per-sorted-particle u32 surface flags (parity output)

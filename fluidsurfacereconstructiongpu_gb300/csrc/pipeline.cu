@@ -2,8 +2,8 @@
 //
 // One frame is one queue of kernels on the caller's stream: spatial hashing
 // (key + stable radix sort + ranges), surface cells, narrow band (bitset +
-// rank directory + band list), field, marching cubes (classify, two scans,
-// valid-cube list, generation).  Sizes the reference reads back after every
+// rank directory + band list), field, marching cubes (classify, one scan
+// for the vertex offsets and the valid-cube list, generation).  Sizes the reference reads back after every
 // scan (ReconstructionCUDA.cu:1164-1171) stay on the device in a Counters
 // block; the host reads that block once at the end of the frame.  When a
 // pooled buffer turned out too small the frame is re-queued with the grown
@@ -175,7 +175,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &qpos,   &valid,   &mean,   &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &valid,   &mean,   &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -247,7 +247,7 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         for (auto& e : h->ev) CK(cudaEventCreate(&e));
     }
     const bool weld = (p.flags & FSR_FLAG_WELD) != 0;
-    uint64_t scan_words = std::max<uint64_t>(scan_scratch_words(nwords), scan_scratch_words(h->cap_band));
+    uint64_t scan_words = std::max<uint64_t>(scan_scratch_words(nwords), mc_offsets_scratch_words(h->cap_band));
     if (weld) {
         scan_words = std::max<uint64_t>(scan_words, scan_scratch_words(h->cap_mesh));
         const uint64_t cm = h->cap_mesh, ts = weld_table_size(h->cap_mesh);
@@ -265,7 +265,6 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
     CK(h->phi.ensure(4ull * h->cap_band));
     CK(h->mc.ensure(4ull * h->cap_band));
     CK(h->vofs.ensure(4ull * h->cap_band));
-    CK(h->qpos.ensure(4ull * h->cap_band));
     CK(h->valid.ensure(4ull * h->cap_valid));
     CK(h->mesh_pos.ensure(12ull * h->cap_mesh));
     CK(h->mesh_nrm.ensure(12ull * h->cap_mesh));
@@ -418,8 +417,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     ma.band = BandView{bits, prefix, phi};
     ma.sv = sv;
     ma.mc = (uint32_t*)h->mc.ptr;
-    ma.vofs = (const uint32_t*)h->vofs.ptr;
-    ma.qpos = (const uint32_t*)h->qpos.ptr;
+    ma.vofs = (uint32_t*)h->vofs.ptr;
     ma.valid = (uint32_t*)h->valid.ptr;
     ma.out_pos = (float*)h->mesh_pos.ptr;
     ma.out_nrm = (float*)h->mesh_nrm.ptr;
@@ -433,11 +431,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     ma.out_key = weld ? (uint64_t*)h->wkey.ptr : nullptr;
     launch_mc_classify(kc, ma, ctr);
     mark(8);
-    CK(scan_u32(ma.mc, (uint32_t*)h->vofs.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_mesh_verts,
-                ScanInput::kLowByte, (uint32_t*)h->scan_tmp.ptr, st));
-    CK(scan_u32(ma.mc, (uint32_t*)h->qpos.ptr, 0, &ctr->n_band, h->cap_band, &ctr->n_valid,
-                ScanInput::kLowByteNonzero, (uint32_t*)h->scan_tmp.ptr, st));
-    launch_valid_list(kc, ma, ctr);
+    launch_mc_offsets(kc, ma, ctr, (uint32_t*)h->scan_tmp.ptr);
     mark(9);
     launch_mc_generate(kc, ma, ctr);
     if (weld) {

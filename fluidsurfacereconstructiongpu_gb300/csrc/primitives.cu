@@ -14,8 +14,6 @@ __device__ __forceinline__ uint32_t scan_load(const uint32_t* in, uint32_t i)
     const uint32_t v = __ldg(in + i);
     if (M == ScanInput::kPopcount) return __popc(v);
     if (M == ScanInput::kNonzero) return v != 0u ? 1u : 0u;
-    if (M == ScanInput::kLowByte) return v & 0xFFu;
-    if (M == ScanInput::kLowByteNonzero) return (v & 0xFFu) != 0u ? 1u : 0u;
     return v;
 }
 
@@ -23,31 +21,6 @@ __device__ __forceinline__ uint32_t count_of(uint32_t n_host, const uint32_t* n_
 {
     const uint32_t n = n_dev ? *n_dev : n_host;
     return n < n_max ? n : n_max;
-}
-
-// Inclusive scan of one value per thread across the block (256 threads).
-__device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t x, uint32_t* warp_sums)
-{
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t s = lane < (kScanThreads / 32) ? warp_sums[lane] : 0u;
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        if (lane < (kScanThreads / 32)) warp_sums[lane] = s;
-    }
-    __syncthreads();
-    const uint32_t add = warp ? warp_sums[warp - 1] : 0u;
-    return x + add;
 }
 
 template <ScanInput M>
@@ -263,10 +236,6 @@ cudaError_t scan_u32(const uint32_t* in, uint32_t* out, uint32_t n_host, const u
     case ScanInput::kValue: launch_scan<ScanInput::kValue>(g, in, out, n_host, n_dev, n_max, total, scratch, stream); break;
     case ScanInput::kPopcount: launch_scan<ScanInput::kPopcount>(g, in, out, n_host, n_dev, n_max, total, scratch, stream); break;
     case ScanInput::kNonzero: launch_scan<ScanInput::kNonzero>(g, in, out, n_host, n_dev, n_max, total, scratch, stream); break;
-    case ScanInput::kLowByte: launch_scan<ScanInput::kLowByte>(g, in, out, n_host, n_dev, n_max, total, scratch, stream); break;
-    case ScanInput::kLowByteNonzero:
-        launch_scan<ScanInput::kLowByteNonzero>(g, in, out, n_host, n_dev, n_max, total, scratch, stream);
-        break;
     }
     return cudaGetLastError();
 }

@@ -17,10 +17,35 @@ constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
 enum class ScanInput : int {
     kValue = 0,          // the element
     kPopcount = 1,       // popcount of the element
-    kNonzero = 2,        // element != 0
-    kLowByte = 3,        // element & 0xFF
-    kLowByteNonzero = 4  // (element & 0xFF) != 0
+    kNonzero = 2         // element != 0
 };
+
+#ifdef __CUDACC__
+// Inclusive scan of one value per thread across the block (256 threads).
+__device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t x, uint32_t* warp_sums)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < (kScanThreads / 32) ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < (kScanThreads / 32)) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t add = warp ? warp_sums[warp - 1] : 0u;
+    return x + add;
+}
+#endif
 
 // Scratch words needed by scan_u32 for up to n_max elements.
 size_t scan_scratch_words(uint64_t n_max);
