@@ -36,6 +36,7 @@ struct GroupArgs {
     const float4* grec;
     const float4* qrec;  // per involved particle: (x~, r2max) (M00, 2M01, 2M02, coef) (M11, 2M12, M22, 0)
     const float4* smoothed;
+    const uint32_t* glist;  // groups holding band vertices
     const uint2* ranges;
     const uint8_t* invol;
     const float* reach;
@@ -572,13 +573,14 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
     const int lane = threadIdx.x & 31;
     WarpSlice& w = slices[threadIdx.x >> 5];
     const uint32_t nb = min(ctr->n_band, a.cap);
-    const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const uint32_t ngroups = ctr->n_groups;  // groups holding band vertices
 
     for (;;) {
-        uint32_t g = 0;
-        if (lane == 0) g = atomicAdd(&ctr->work_field, 1u);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= ngroups) break;
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(&ctr->work_field, 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= ngroups) break;
+        const uint32_t g = a.glist[k];
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
         bool tables = false;
@@ -796,15 +798,16 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
     const int lane = threadIdx.x & 31;
     IsoSlice& w = slices[threadIdx.x >> 5];
     const uint32_t nb = min(ctr->n_band, a.cap);
-    const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const uint32_t ngroups = ctr->n_groups;  // groups holding band vertices
     const float cr = cull_radius(a.h, a.sp.cs), cr2 = cr * cr;
     constexpr int kSums = TC01 ? 1 : 4;
 
     for (;;) {
-        uint32_t g = 0;
-        if (lane == 0) g = atomicAdd(&ctr->work_field, 1u);
-        g = __shfl_sync(0xffffffffu, g, 0);
-        if (g >= ngroups) break;
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(&ctr->work_field, 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= ngroups) break;
+        const uint32_t g = a.glist[k];
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
         // rows of the +-1 window (clamped as window() clamps), z then y
@@ -1339,6 +1342,7 @@ void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
     a.grec = f.grec;
     a.qrec = f.qrec;
     a.smoothed = f.smoothed;
+    a.glist = f.glist;
     a.ranges = f.ranges;
     a.invol = f.invol;
     a.reach = f.cell_rmax;

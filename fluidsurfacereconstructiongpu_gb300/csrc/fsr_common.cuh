@@ -45,7 +45,8 @@ struct Counters {
     uint32_t work_field;     // next window group of the anisotropic field (dynamic scheduling)
     uint32_t work_adjoint;   // the same for its adjoint
     uint32_t n_weld;         // welded mesh vertices (FSR_FLAG_WELD)
-    uint32_t pad[2];
+    uint32_t n_groups;       // window groups holding band vertices (the field's work list)
+    uint32_t pad[1];
 };
 
 // Rank directory over the band bitset: rank(v) = number of band vertices

@@ -71,6 +71,7 @@ struct fsr_handle {
     fsr::DevBuf ranges, occ, surf, invol, cell_rmax;
     // vertex-sized
     fsr::DevBuf bits, prefix, scan_tmp;
+    fsr::DevBuf gflag, glist;            // window groups holding band vertices: flags, list
     // band-sized
     fsr::DevBuf sv, phi, mc, vofs, valid;
     // mesh

@@ -373,23 +373,61 @@ __global__ void k_band_stamp(const float4* __restrict__ sorted, const uint32_t* 
 }
 
 // compactSurfaceVertex (cu:293-304) over the bitset: every set bit writes
-// its vertex id at its rank.
+// its vertex id at its rank.  The band vertices also mark their window
+// groups (the spatial cell a vertex's FP32 position falls in, as the grouped
+// field kernels' group boxes have it); the first mark of a group appends it
+// to the group list.  A word is cut into its grid rows; per row the groups
+// from the first set bit's to the last's are marked (a superset at worst:
+// a marked group without band vertices is found empty).
 __global__ void k_band_list(const uint32_t* __restrict__ bits, const uint32_t* __restrict__ prefix,
-                            uint32_t nwords, uint32_t* __restrict__ sv, uint32_t cap, Counters* ctr)
+                            uint32_t nwords, uint32_t* __restrict__ sv, uint32_t cap, GroupMark gm, Counters* ctr)
 {
+    const uint32_t kx = gm.sp.res[0] + 1, ky = gm.sp.res[1] + 1;
+    const uint32_t rx = gm.sc.res[0], rxy = gm.sc.res[0] * gm.sc.res[1];
     const uint32_t nb = ctr->n_band;
     if (blockIdx.x == 0 && threadIdx.x == 0 && nb > cap) {
         atomicOr(&ctr->overflow, 1u);
         atomicMax(&ctr->need_band, nb);
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += gridDim.x * blockDim.x) {
-        uint32_t w = bits[i];
+        const uint32_t w0 = bits[i];
+        if (w0 == 0u) continue;
+        uint32_t w = w0;
         uint32_t r = prefix[i];
         while (w) {
             const uint32_t b = __ffs(w) - 1;
             w &= w - 1;
             if (r < cap) sv[r] = (i << 5) | b;
             ++r;
+        }
+        // the word's rows: bits [s, e) lie in row (y, z) from column x on
+        const uint32_t v0 = i << 5;
+        uint32_t z = v0 / rxy, y = (v0 - z * rxy) / rx, x = v0 - z * rxy - y * rx;
+        uint32_t last = 0xffffffffu;
+        for (uint32_t s = 0; s < 32u;) {
+            const uint32_t len = min(32u - s, rx - x);
+            const uint32_t seg = w0 & ((len == 32u ? 0xffffffffu : ((1u << len) - 1u)) << s);
+            if (seg) {
+                const uint32_t xf = x + (uint32_t)(__ffs(seg) - 1) - s, xl = x + (31u - (uint32_t)__clz(seg)) - s;
+                const int cf = clampi(cell1(vpos1(xf, gm.sc.min[0], gm.sc.cs), gm.sp.min[0], gm.sp.cs), 0, (int)kx - 1);
+                const int cl = clampi(cell1(vpos1(xl, gm.sc.min[0], gm.sc.cs), gm.sp.min[0], gm.sp.cs), 0, (int)kx - 1);
+                const int cy = clampi(cell1(vpos1(y, gm.sc.min[1], gm.sc.cs), gm.sp.min[1], gm.sp.cs), 0, (int)ky - 1);
+                const int cz = clampi(cell1(vpos1(z, gm.sc.min[2], gm.sc.cs), gm.sp.min[2], gm.sp.cs), 0,
+                                      (int)gm.sp.res[2]);
+                for (int cx = cf; cx <= cl; ++cx) {
+                    const uint32_t g = (uint32_t)cx + kx * ((uint32_t)cy + ky * (uint32_t)cz);
+                    if (g != last) {
+                        last = g;
+                        if (atomicExch(gm.gflag + g, 1u) == 0u) gm.glist[atomicAdd(&ctr->n_groups, 1u)] = g;
+                    }
+                }
+            }
+            s += len;
+            x = 0;
+            if (++y == gm.sc.res[1]) {
+                y = 0;
+                ++z;
+            }
         }
     }
 }
@@ -1023,9 +1061,9 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
 }
 
 void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
-                      uint32_t* sv, uint32_t cap, Counters* ctr)
+                      uint32_t* sv, uint32_t cap, const GroupMark& gm, Counters* ctr)
 {
-    k_band_list<<<persistent_blocks(c, nwords, 16), kThreads, 0, c.stream>>>(bits, prefix, nwords, sv, cap, ctr);
+    k_band_list<<<persistent_blocks(c, nwords, 16), kThreads, 0, c.stream>>>(bits, prefix, nwords, sv, cap, gm, ctr);
     ++g_launches;
 }
 

@@ -47,8 +47,17 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
                        const uint8_t* surf, const uint8_t* psurf, uint32_t n, const Grid& sc,
                        float thr, uint32_t* bits, Counters* ctr);
 
+// The band list, and the list of the window groups (spatial cells of the
+// (res + 1)^3 grid the grouped field kernels walk) that hold band vertices:
+// glist[0 .. ctr->n_groups), in no particular order; gflag (one word per
+// group) must start at zero.
+struct GroupMark {
+    Grid sp, sc;
+    uint32_t* gflag;
+    uint32_t* glist;
+};
 void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
-                      uint32_t* sv, uint32_t cap, Counters* ctr);
+                      uint32_t* sv, uint32_t cap, const GroupMark& gm, Counters* ctr);
 
 struct IsoFieldArgs {
     Grid sp, sc;
@@ -58,6 +67,7 @@ struct IsoFieldArgs {
     const uint32_t* sv;
     float* phi;
     float4* mv;  // optional (ZB05): per band vertex (mean - v, weight sum), kept for the backward pass
+    const uint32_t* glist;  // groups holding band vertices (ctr->n_groups of them)
     float h, h2, inv_h2, rp;
     uint32_t cap;
 };
@@ -107,6 +117,7 @@ struct AnisoFieldArgs {
     const float* cell_rmax;
     const uint32_t* sv;
     float* phi;
+    const uint32_t* glist;  // groups holding band vertices (ctr->n_groups of them)
     float sigma;
     uint32_t cap;
 };

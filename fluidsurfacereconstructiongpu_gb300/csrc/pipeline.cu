@@ -174,7 +174,7 @@ fsr_handle::~fsr_handle()
 std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
-            &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
+            &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &gflag, &glist, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
             &valid,   &mean,   &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
@@ -228,6 +228,9 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
     CK(h->surf.ensure(C));
     CK(h->bits.ensure(4ull * nwords + 4));
     CK(h->prefix.ensure(4ull * nwords + 4));
+    const uint64_t G = (uint64_t)(fp.sp.res[0] + 1) * (fp.sp.res[1] + 1) * (fp.sp.res[2] + 1);
+    CK(h->gflag.ensure(4ull * G));
+    CK(h->glist.ensure(4ull * G));
     CK(h->ctr.ensure(sizeof(Counters)));
     if (yu13) {
         CK(h->invol.ensure(C));
@@ -343,7 +346,10 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     CK(scan_u32(bits, prefix, nwords, nullptr, nwords, &ctr->n_band, ScanInput::kPopcount,
                 (uint32_t*)h->scan_tmp.ptr, st));
     uint32_t* sv = (uint32_t*)h->sv.ptr;
-    launch_band_list(kc, bits, prefix, nwords, sv, h->cap_band, ctr);
+    const uint64_t G = (uint64_t)(sp.res[0] + 1) * (sp.res[1] + 1) * (sp.res[2] + 1);
+    CK(cudaMemsetAsync(h->gflag.ptr, 0, 4ull * G, st));
+    launch_band_list(kc, bits, prefix, nwords, sv, h->cap_band,
+                     GroupMark{sp, sc, (uint32_t*)h->gflag.ptr, (uint32_t*)h->glist.ptr}, ctr);
     mark(4);
 
     // ---- field
@@ -388,6 +394,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.sv = sv;
         fa.phi = phi;
         fa.sigma = ca.sigma;
+        fa.glist = (const uint32_t*)h->glist.ptr;
         fa.cap = h->cap_band;
         launch_field_aniso_grouped(kc, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr);
     } else {
@@ -406,6 +413,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
         fa.inv_h2 = 1.0f / h2;
         fa.rp = hdr.particle_radius;
         fa.mv = p.method == FSR_METHOD_TC01 ? nullptr : (float4*)h->mv.ptr;
+        fa.glist = (const uint32_t*)h->glist.ptr;
         fa.cap = h->cap_band;
         launch_field_iso_grouped(kc, p.method == FSR_METHOD_TC01, fa, BandView{bits, prefix, phi}, p.grid_ratio, ctr);
     }
