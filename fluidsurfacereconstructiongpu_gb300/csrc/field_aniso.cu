@@ -647,14 +647,16 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                 const int cell = chunk_cell(cb, lane, w.cpre, w.ncells, k0);
                 if (j < total_inv) {
                     const uint32_t i = w.cstart[cell] + (j - w.cpre[cell]);
+                    // the three loads in flight together (most candidates are kept)
                     const float4* qsrc = a.qrec + 3ull * i;
                     r0 = __ldg(qsrc);
+                    const float4 r1 = __ldg(qsrc + 1), r2 = __ldg(qsrc + 2);
                     keep = reaches(r0, pl, ph);
                     if (keep) {
                         float4* dst = w.rec + 3 * lane;
                         dst[0] = r0;
-                        dst[1] = __ldg(qsrc + 1);
-                        dst[2] = __ldg(qsrc + 2);
+                        dst[1] = r1;
+                        dst[2] = r2;
                     }
                 }
                 const uint32_t any = __ballot_sync(0xffffffffu, keep);
