@@ -552,9 +552,14 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
 // when the covariance's condition number exceeds 1e4.
 // Output record per particle: (x,y,z smoothed, r2max) (G row 0, coef)
 // (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
-__global__ void __launch_bounds__(kThreads, 4) k_cov(CovArgs a, Counters* ctr)
+// Blocks of two warps: a warp without involved particles exits at once, and
+// a small block gives its registers back as soon as its two warps are done,
+// so the working warps' blocks fill the SM.
+constexpr int kCovThreads = 64;
+
+__global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ctr)
 {
-    __shared__ float4 s_q[kThreads];  // 32 staged candidates per warp
+    __shared__ float4 s_q[kCovThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     bool act = t < a.n && a.invol[a.skeys[t]];
     warp_count(&ctr->n_involved, act);
@@ -1090,7 +1095,7 @@ void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
     a.R_rcp = 1.0f / a.R;
     a.R_le2 = sqrt_threshold(a.R, true);
     a.coop_ok = (a.R + a.R * 1.0001f + 1e-4f * a.sp.cs) < 2.0f * a.sp.cs * 0.9999f ? 1 : 0;
-    k_cov<<<blocks_for(a.n), kThreads, 0, c.stream>>>(a, ctr);
+    k_cov<<<blocks_for(a.n, kCovThreads), kCovThreads, 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
 
