@@ -479,9 +479,14 @@ __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool 
     }
 }
 
-__global__ void __launch_bounds__(kT, 3) k_cov_backward(BwdArgs a, CovArgs f)
+// Blocks of two warps (at the registers of 3 blocks of 256 threads per SM):
+// a warp without work exits at once, and a small block gives its registers
+// back as soon as its two warps are done.
+constexpr int kCovBT = 64;
+
+__global__ void __launch_bounds__(kCovBT, 12) k_cov_backward(BwdArgs a, CovArgs f)
 {
-    __shared__ float4 s_q[kT];  // 32 staged particles per warp
+    __shared__ float4 s_q[kCovBT];  // 32 staged particles per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < f.n;
     float4 gmo = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -665,7 +670,7 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
         } else {
             k_field_backward_aniso<<<nblk(a.n), kT, 0, c.stream>>>(a);
         }
-        k_cov_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, *cov);
+        k_cov_backward<<<(unsigned)std::max<uint64_t>(1, (a.n + kCovBT - 1) / kCovBT), kCovBT, 0, c.stream>>>(a, *cov);
         // warps may walk the union of their windows when the cull radius stays below 2 cells
         const int smooth_coop = (R * 1.0001f + 1e-4f * cov->sp.cs) < 2.0f * cov->sp.cs * 0.9999f ? 1 : 0;
         k_smooth_backward<<<nblk(a.n), kT, 0, c.stream>>>(a, cov->sorted, cov->mean, cov->ranges, cov->sp, a.n, R,
