@@ -40,6 +40,9 @@ WORKLOADS = {
                       aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10, iso=0.0),
     # the same frame with the plain ZB05 path (grid spacing 0.5r: ratio 8 at cell = h)
     "plain1m": dict(kind="dam_break", n=1 << 20, r=0.004, seed=2, method="zb05", grid_ratio=8),
+    # the plain and Akinci12 paths at 2^18 particles (profiling captures)
+    "plain256k": dict(kind="dam_break", n=1 << 18, r=0.004, seed=2, method="zb05", grid_ratio=8),
+    "akinci256k": dict(kind="dam_break", n=1 << 18, r=0.004, seed=2, method="akinci12", grid_ratio=8),
     # 32^3 lattice, ZB05, grid spacing 0.5r
     "plain32k": dict(kind="lattice", n_side=32, r=0.0125, seed=1, method="zb05", grid_ratio=8),
 }
@@ -79,21 +82,16 @@ def cpu_kind():
     return "oracle32", "port"
 
 
-def cpu_frame(w, fr, field_stride):
-    """One CPU frame; returns (seconds, description of the sample)."""
+def cpu_frame(w, fr):
+    """One whole CPU frame (every stage, the field at every band vertex);
+    returns (seconds, kind, threads, description of the sample)."""
     from oracle import pipeline as P
     kind, label = cpu_kind()
     threads = P.set_threads(kind, os.cpu_count() or 1)
-    times = {}
     t0 = time.perf_counter()
-    P.run_frame(kind, fr.pos, fr.density, fr.bbox_min, fr.bbox_max, oracle_params(w, fr), times=times,
-                field_stride=field_stride)
+    P.run_frame(kind, fr.pos, fr.density, fr.bbox_min, fr.bbox_max, oracle_params(w, fr))
     wall = time.perf_counter() - t0
-    est = wall + times.get("_unsampled_extra", 0.0)
-    sample = (f"one full {fr.n}-particle frame, all stages; field evaluated at every {field_stride}-th band "
-              f"vertex and its time scaled by {field_stride}") if field_stride > 1 else \
-        f"one full {fr.n}-particle frame, all stages"
-    return est, label, threads, sample
+    return wall, label, threads, f"one whole {fr.n}-particle frame, every stage, timed end to end"
 
 
 class ClockSampler:
@@ -162,6 +160,7 @@ def committed_traffic(kernel_key):
     return d.get(kernel_key)
 
 
+PAIR_FLOPS = {"yu13": 33, "zb05": 16, "tc01": 12, "smooth": 14, "cov": 25}  # FP32 flops per pair
 BATCH = dict(frames=64, n_lo=20000, n_hi=400000, seed=3, methods=("akinci12", "zb05", "yu13"),
              # grid spacing 0.5r everywhere (ratio 8 at cell = h); the anisotropic
              # frames use the 1M anisotropic frame's settings
@@ -183,16 +182,16 @@ def batch_frames(cfg=BATCH):
     return out
 
 
-def run_batch_leg(dev, stream, steps, warmup, flush):
+def run_batch_leg(dev, stream, steps, warmup, flush, cfg=BATCH):
     """The batched forward (one graph launch for all frames) against the
     single-frame path on the same frames; both device-resident."""
     import torch
     from fluidsurfacereconstructiongpu_gb300 import api
-    frames = batch_frames()
+    frames = batch_frames(cfg)
     total = sum(fr.n for _, fr in frames)
     args = [(m, torch.from_numpy(fr.pos).to(dev), torch.from_numpy(fr.density).to(dev), api.header_of(fr))
             for m, fr in frames]
-    b = api.Batch(dev.index or 0, params=BATCH["params"])
+    b = api.Batch(dev.index or 0, params=cfg["params"])
     b.reconstruct(args, stream=stream)  # plan + autotune
     for _ in range(max(warmup - 1, 1)):
         b.reconstruct(args, stream=stream)
@@ -209,7 +208,7 @@ def run_batch_leg(dev, stream, steps, warmup, flush):
     tun = b.tuning()
     launches = int(tun.kernels_per_launch)
     b.close()
-    recs = {m: api.Reconstructor(m, dev.index or 0, **BATCH["params"][m]) for m in set(m for m, _ in frames)}
+    recs = {m: api.Reconstructor(m, dev.index or 0, **cfg["params"][m]) for m in set(m for m, _ in frames)}
     for _ in range(warmup):
         for m, x, d, hdr in args:
             recs[m].reconstruct(x, d, hdr, stream)
@@ -227,8 +226,8 @@ def run_batch_leg(dev, stream, steps, warmup, flush):
     for r in recs.values():
         r.close()
     tb, ts = float(np.mean(ms_b)), float(np.mean(ms_s))
-    return {"frames": len(frames), "particles": total, "methods": {m: sum(1 for q, _ in frames if q == m)
-                                                                    for m in BATCH["methods"]},
+    return {"frames": len(frames), "particle_range": [cfg["n_lo"], cfg["n_hi"]], "particles": total,
+            "methods": {m: sum(1 for q, _ in frames if q == m) for m in cfg["methods"]},
             "value": total / (tb / 1e3), "ms_per_step": tb, "single_frame_value": total / (ts / 1e3),
             "single_frame_ms": ts, "speedup_vs_single_frame": ts / tb, "lanes": int(tun.lanes),
             "grid_div": int(tun.grid_div), "autotune_candidates": int(tun.n_candidates),
@@ -251,20 +250,19 @@ def dist_setup(args):
 
 
 def run_reference(args, w, fr):
-    """--impl reference: the reference's pipeline on the host cores."""
+    """--impl reference: the reference's pipeline on the host cores, whole
+    frames (every stage, the field at every band vertex), W warm-up frames
+    (at most one: a CPU frame has nothing to warm) and K timed frames."""
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
         return
-    stride = args.cpu_field_stride
-    # a CPU frame takes seconds: at most 1 warm-up and 5 timed frames keep the
-    # run within a few minutes (the line reports the counts actually run)
-    warmup, steps = min(args.warmup, 1), max(1, min(args.steps, 5))
+    warmup, steps = min(args.warmup, 1), max(1, args.steps)
     for _ in range(warmup):
-        cpu_frame(w, fr, max(stride, 8))
+        cpu_frame(w, fr)
     secs = []
     label = threads = sample = None
     for _ in range(steps):
-        s, label, threads, sample = cpu_frame(w, fr, stride)
+        s, label, threads, sample = cpu_frame(w, fr)
         secs.append(s)
     t = float(np.mean(secs))
     val = fr.n / t
@@ -396,6 +394,134 @@ def run_io_leg(args, w):
         shutil.rmtree(d, ignore_errors=True)
 
 
+def pipeline_bytes(method, n, C, V, B, I, Q, T):
+    """Algorithmic compulsory bytes of one forward frame and of its backward
+    pass: every input read once, every output written once, every
+    unavoidable intermediate written and read once (FP32 / u32)."""
+    fwd = (16 * n + 16 * n + 16 * n + 8 * C + C / 8)      # hash + sort + ranges
+    fwd += 8 * C + n / 8                                   # surface / involved flags
+    fwd += V / 8 + V / 8 + 4 * B                           # band bitset, its scan, band list
+    if method == "yu13":
+        fwd += 12 * n + 12 * n                             # smoothing
+        fwd += 12 * I + 36 * I + 4 * I                     # covariance + G
+        fwd += 16 * n + 36 * I + 4 * B                     # field
+    else:
+        fwd += 16 * n + 4 * B                              # field
+    fwd += 4 * B + 4 * B + 4 * Q                           # MC classify + compaction
+    fwd += 4 * B + 24 * 3 * T                              # MC generation
+    bwd = fwd + 24 * 3 * T + 16 * n + (2 * 36 * I if method == "yu13" else 0)
+    return float(fwd), float(bwd)
+
+
+def time_steps(fn, stream, steps, flush):
+    """CUDA-event time of each of `steps` calls of fn on `stream`, L2 flushed
+    (outside the events) before each."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def make_backward(rec, stream, dev, n):
+    """fsr_backward of a fixed dL/d(mesh): the gradient of the mean squared
+    deviation of the mesh vertices' distances to their centroid."""
+    import ctypes as _ct
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import _native
+    mpos, _ = rec.mesh_tensors(stream)
+    c = mpos.mean(dim=0)
+    d = mpos - c
+    rr = d.norm(dim=1, keepdim=True).clamp_min(1e-12)
+    gmesh = (2.0 * (rr - rr.mean()) / rr / mpos.shape[0] * d).contiguous()
+    gx = torch.empty((n, 3), dtype=torch.float32, device=dev)
+
+    def bwd():
+        _native.check(_native.lib.fsr_backward(rec._h, _ct.c_void_p(gmesh.data_ptr()), _ct.c_void_p(gx.data_ptr()),
+                                               None, _ct.c_void_p(stream.cuda_stream)), rec._h)
+    return bwd
+
+
+def frame_leg(w, fr, dev, stream, steps, warmup, flush, fp32_tflops, peak_gbs, backward=True):
+    """One workload on the GPU: the frame timed clean (no instrumentation),
+    then stage times from a separate instrumented pass, the pair counts of
+    the neighbour-sum stages, forward + backward, and the rooflines."""
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api, _native
+    hdr = api.header_of(fr)
+    xyz = torch.from_numpy(fr.pos).to(dev)
+    den = torch.from_numpy(fr.density).to(dev)
+    rec = api.Reconstructor(w["method"], dev.index or 0, **recon_kwargs(w))
+    for _ in range(warmup):
+        rec.reconstruct(xyz, den, hdr, stream)
+    ms = time_steps(lambda: rec.reconstruct(xyz, den, hdr, stream), stream, steps, flush)
+    st = rec.stats()
+    t = float(np.mean(ms)) / 1e3
+    out = {"workload": w, "particles": fr.n, "ms_per_step": t * 1e3, "value": fr.n / t,
+           "band_vertices": int(st.n_band_vertices), "triangles": int(st.n_mesh_vertices) // 3,
+           "involved_particles": int(st.n_involved_particles), "fp64_fallbacks": int(st.n_fp64_fallbacks),
+           "scalar_grid": list(st.scalar_res), "launches_per_frame": int(st.n_kernel_launches)}
+    # forward + backward (neighbour lists recomputed by the adjoints)
+    if backward:
+        bwd = make_backward(rec, stream, dev, fr.n)
+        for _ in range(warmup):
+            rec.reconstruct(xyz, den, hdr, stream)
+            bwd()
+        msfb = time_steps(lambda: (rec.reconstruct(xyz, den, hdr, stream), bwd()), stream, steps, flush)
+        msb = time_steps(bwd, stream, steps, flush)
+        out["fwd_bwd"] = {"value": fr.n / (float(np.mean(msfb)) / 1e3), "ms_per_step": float(np.mean(msfb)),
+                          "backward_ms": float(np.mean(msb)),
+                          "backward_launches": int(rec.stats().n_backward_launches)}
+    # device memory of the leg: the library's pools plus the caller's inputs
+    # and the backward pass's dL/dmesh and dL/dx buffers
+    out["device_bytes"] = int(rec.stats().device_bytes)
+    out["peak_device_bytes"] = out["device_bytes"] + 16 * fr.n + \
+        ((12 * fr.n + 12 * int(st.n_mesh_vertices)) if backward else 0)
+    pc = rec.pair_counts(stream)
+    rec.close()
+    # stage times: a separate handle with per-stage events
+    rst = api.Reconstructor(w["method"], dev.index or 0, stage_timing=True, **recon_kwargs(w))
+    for _ in range(warmup):
+        rst.reconstruct(xyz, den, hdr, stream)
+    stage = np.zeros(_native.NUM_STAGES)
+    for _ in range(steps):
+        flush.zero_()
+        rst.reconstruct(xyz, den, hdr, stream)
+        stage += np.array(list(rst.stats().stage_ms))
+    rst.close()
+    stage /= steps
+    out["stage_ms"] = {k: round(float(v), 4) for k, v in zip(_native.STAGE_NAMES, stage)}
+    # rooflines: the whole pipeline against HBM, the pair kernels against FP32
+    C = int(np.prod(st.spatial_res))
+    V = int(np.prod(st.scalar_res))
+    fb, bb = pipeline_bytes(w["method"], fr.n, C, V, out["band_vertices"], out["involved_particles"],
+                            int(st.n_valid_cubes), out["triangles"])
+    out["pipeline_roofline"] = {"bound": "hbm", "unit": "GB/s", "peak": peak_gbs,
+                                "fwd": {"bytes": fb, "achieved": fb / t / 1e9, "frac": fb / t / 1e9 / peak_gbs}}
+    if backward:
+        tfb = out["fwd_bwd"]["ms_per_step"] / 1e3
+        out["pipeline_roofline"]["fwd_bwd"] = {"bytes": bb, "achieved": bb / tfb / 1e9,
+                                               "frac": bb / tfb / 1e9 / peak_gbs}
+    fp = {}
+    kinds = [("field", "field", PAIR_FLOPS[w["method"]] if w["method"] in PAIR_FLOPS else 16)]
+    if w["method"] == "yu13":
+        kinds += [("smoothing", "smooth", PAIR_FLOPS["smooth"]), ("covariance", "cov", PAIR_FLOPS["cov"])]
+    for stage_name, key, flops in kinds:
+        ms_k = out["stage_ms"][stage_name]
+        contrib, cand = pc[key + "_contributing"], pc[key + "_candidates"]
+        ach = contrib * flops / (ms_k / 1e3) / 1e12 if ms_k > 0 else 0.0
+        fp[stage_name] = {"candidate_pairs": cand, "contributing_pairs": contrib, "flops_per_pair": flops,
+                          "stage_ms": ms_k, "achieved_tflops": ach, "peak_tflops": fp32_tflops,
+                          "frac": ach / fp32_tflops if fp32_tflops else None}
+    out["fp32_pipe"] = fp
+    out["pair_counts"] = pc
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -403,25 +529,28 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="aniso1m")
-    ap.add_argument("--cpu-field-stride", type=int, default=4,
-                    help="CPU baseline: evaluate the field at every k-th band vertex and scale its time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-backward", action="store_true", help="skip the forward+backward leg")
-    ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames legs")
+    ap.add_argument("--no-extra", action="store_true", help="skip the plain-path and 8M legs")
     ap.add_argument("--compute-density", action="store_true",
                     help="frames without densities: the GPU computes them (FSR_FLAG_COMPUTE_DENSITY); "
                          "no backward or batch legs")
     ap.add_argument("--io", action="store_true",
                     help="time the file-driven loop (.xyz in, .obj out) instead of the in-memory frame")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: W warm-up frames, then one frame and one backward pass, nothing else")
+    ap.add_argument("--weld", action="store_true", help="profiling run: weld the mesh (FSR_FLAG_WELD)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
-    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" and not args.profile else args.warmup
     if args.io:
         run_io_leg(args, w)
         return
     if args.compute_density:
         args.no_backward = True
         args.no_batch = True
+        args.no_extra = True
 
     if args.impl == "reference":
         fr = make_frame(w)
@@ -430,6 +559,24 @@ def main():
 
     import torch
     from fluidsurfacereconstructiongpu_gb300 import api, _native
+
+    if args.profile:
+        torch.cuda.set_device(0)
+        fr = make_frame(w)
+        rec = api.Reconstructor(w["method"], 0, compute_density=args.compute_density, weld=args.weld,
+                                **recon_kwargs(w))
+        xyz = torch.from_numpy(fr.pos).cuda()
+        den = None if args.compute_density else torch.from_numpy(fr.density).cuda()
+        hdr = api.header_of(fr)
+        stream = torch.cuda.current_stream()
+        for _ in range(args.warmup + 1):
+            rec.reconstruct(xyz, den, hdr, stream)
+        if not args.no_backward and not args.compute_density:
+            make_backward(rec, stream, torch.device("cuda", 0), fr.n)()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.workload, "launches_per_frame": int(rec.stats().n_kernel_launches)}))
+        rec.close()
+        return
 
     world, rank, local, pg = dist_setup(args)
     torch.cuda.set_device(local)
@@ -441,90 +588,54 @@ def main():
     # CPU baseline first (rank 0, N = 1), before any GPU work
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and fr.n <= (1 << 21):
-        s, label, threads, sample = cpu_frame(w, fr, args.cpu_field_stride)
-        cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample}
+        s, label, threads, sample = cpu_frame(w, fr)
+        cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample,
+               "ms_per_frame": s * 1e3}
 
-    rec = api.Reconstructor(w["method"], local, stage_timing=True, compute_density=args.compute_density,
-                            **recon_kwargs(w))
+    rec = api.Reconstructor(w["method"], local, compute_density=args.compute_density, **recon_kwargs(w))
     hdr = api.header_of(fr)
     xyz = torch.from_numpy(fr.pos).to(dev)
     den = None if args.compute_density else torch.from_numpy(fr.density).to(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
-    launches0 = None
     for _ in range(args.warmup):
         rec.reconstruct(xyz, den, hdr, stream)
-    st = rec.stats()
-    n_launch_per_frame = getattr(_native, "KERNELS_PER_FRAME", {}).get(w["method"])
 
+    # the headline: whole frames, no per-stage events, nothing read back
+    # between steps but what the frame itself reads (its sizes)
     if pg:
         pg.barrier()
     torch.cuda.synchronize(dev)
     sampler = ClockSampler(local)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stage = np.zeros(_native.NUM_STAGES)
-    for k in range(args.steps):
-        flush.zero_()  # evict L2 between steps (outside the timed events)
-        starts[k].record(stream)
-        rec.reconstruct(xyz, den, hdr, stream)
-        ends[k].record(stream)
-        s = rec.stats()
-        stage += np.array(list(s.stage_ms))
-    torch.cuda.synchronize(dev)
-    ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    ms = time_steps(lambda: rec.reconstruct(xyz, den, hdr, stream), stream, args.steps, flush)
     t_step = float(np.mean(ms)) / 1e3
-    st = rec.stats()
-    stage /= args.steps
     if pg:
         tt = torch.tensor([t_step], dtype=torch.float64, device=dev)
         pg.all_reduce(tt, op=pg.ReduceOp.MAX)
         t_step = float(tt.item())
     value = fr.n * world / t_step
+    st = rec.stats()
+    n_launch = int(st.n_kernel_launches)
 
-    # forward + backward: the same frame, then dL/dx from a fixed dL/d(mesh) (the
-    # gradient of the mean squared distance of the mesh vertices to a sphere)
-    fb = None
-    if not args.no_backward:
-        mpos, _ = rec.mesh_tensors(stream)
-        c = mpos.mean(dim=0)
-        d = mpos - c
-        rr = d.norm(dim=1, keepdim=True).clamp_min(1e-12)
-        gmesh = (2.0 * (rr - rr.mean()) / rr / mpos.shape[0] * d).contiguous()
-        gx = torch.empty((fr.n, 3), dtype=torch.float32, device=dev)
-        import ctypes as _ct
-
-        def bwd():
-            _native.check(_native.lib.fsr_backward(rec._h, _ct.c_void_p(gmesh.data_ptr()), _ct.c_void_p(gx.data_ptr()),
-                                                   None, _ct.c_void_p(stream.cuda_stream)), rec._h)
-        for _ in range(args.warmup):
-            rec.reconstruct(xyz, den, hdr, stream)
-            bwd()
-        torch.cuda.synchronize(dev)
-        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-        for k in range(args.steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            rec.reconstruct(xyz, den, hdr, stream)
-            ev[k][1].record(stream)
-            bwd()
-            ev[k][2].record(stream)
-        torch.cuda.synchronize(dev)
-        t_fb = float(np.mean([a.elapsed_time(c_) for a, _, c_ in ev])) / 1e3
-        t_b = float(np.mean([b.elapsed_time(c_) for _, b, c_ in ev])) / 1e3
-        if pg:
-            tt = torch.tensor([t_fb], dtype=torch.float64, device=dev)
-            pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-            t_fb = float(tt.item())
-        n_bwd = int(rec.stats().n_backward_launches)
-        fb = {"value": fr.n * world / t_fb, "unit": "particles/s", "ms_per_step": t_fb * 1e3,
-              "backward_ms": t_b * 1e3, "backward_launches_per_step": n_bwd,
-              "loss": "mean over mesh vertices of (|v - c| - mean |v - c|)^2, c = mesh centroid (gradient fixed)"}
-        st = rec.stats()
-
+    # the same workload's detail: stage times, pair counts, backward, rooflines
+    fp32 = ctypes_fp32_rate(local)
+    peak, peak_kind = measured_peaks()
+    detail = None
+    if not args.compute_density:
+        detail = frame_leg(w_rank, fr, dev, stream, args.steps, args.warmup, flush, fp32, peak,
+                           backward=not args.no_backward)
+    extra = {}
+    if not args.no_extra and world == 1 and args.workload == "aniso1m":
+        for name in ("plain1m", "aniso8m"):
+            wx = WORKLOADS[name]
+            frx = make_frame(wx)
+            extra[name] = frame_leg(wx, frx, dev, stream, min(args.steps, 10), args.warmup, flush, fp32, peak)
+            del frx
     batched = None
     if not args.no_batch:
-        batched = run_batch_leg(dev, stream, args.steps, args.warmup, flush)
+        batched = run_batch_leg(dev, stream, min(args.steps, 10), args.warmup, flush)
+        small = dict(BATCH, n_lo=20000, n_hi=60000, seed=5)
+        batched["small_frames"] = run_batch_leg(dev, stream, min(args.steps, 10), args.warmup, flush, small)
     clocks = sampler.stop()  # sampled over every timed GPU leg above
 
     # end to end through the host API: pinned inputs in, mesh out, every step
@@ -553,34 +664,45 @@ def main():
     h2d = fr.n * (12 if args.compute_density else 16)
     d2h = int(nvo.value) * 24 + 64
 
-    # roofline of the dominant kernel (the field stage)
-    field_ms = float(stage[7])
-    n_inv = int(st.n_involved_particles)
-    B = int(st.n_band_vertices)
-    alg_bytes = 16 * fr.n + 36 * n_inv + 8 * B  # smoothed particles + G read once, band ids read, field written
-    peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (field_ms / 1e3) / 1e9
-    tr = committed_traffic(f"{w['method']}_field_bytes_per_band_vertex")
-    roofline = {"bound": "hbm", "kernel": "k_field_aniso_grouped" if w["method"] == "yu13" else "k_field_iso",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": peak_kind, "traffic": (tr * B if tr else None),
-                "algorithmic_bytes": alg_bytes, "launch_ms": field_ms}
+    # roofline of the dominant kernel (the field), from the instrumented pass
+    roofline = None
+    if detail is not None:
+        field_ms = detail["stage_ms"]["field"]
+        n_inv = detail["involved_particles"]
+        B = detail["band_vertices"]
+        if w["method"] == "yu13":
+            alg_bytes = 16 * fr.n + 36 * n_inv + 8 * B  # smoothed particles + G read once, band ids read, field written
+        else:
+            alg_bytes = 16 * fr.n + 8 * B
+        achieved = alg_bytes / (field_ms / 1e3) / 1e9
+        tr = committed_traffic(f"{w['method']}_field_bytes_per_band_vertex")
+        roofline = {"bound": "hbm", "kernel": "k_field_aniso_grouped" if w["method"] == "yu13"
+                    else "k_field_iso_grouped", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": (tr * B if tr else None),
+                    "algorithmic_bytes": alg_bytes, "launch_ms": field_ms,
+                    "note": "compute-bound: the FP32-pipe fraction (fp32_pipe) is the binding roofline"}
 
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": f"synthetic ({fr.name}, seeded; L2 flushed between steps)",
             "config": {"workload": args.workload, "particles": fr.n, "method": w["method"],
-                       "band_vertices": B, "triangles": int(st.n_mesh_vertices) // 3,
-                       "device_bytes": int(rec.stats().device_bytes), "fp64_fallbacks": int(st.n_fp64_fallbacks),
+                       "band_vertices": int(st.n_band_vertices), "triangles": int(st.n_mesh_vertices) // 3,
+                       "device_bytes": int(st.device_bytes), "fp64_fallbacks": int(st.n_fp64_fallbacks),
                        "scalar_grid": list(st.scalar_res), "l2": "flushed (256 MB write) between steps",
                        "densities": "computed on the GPU (SPH, poly6)" if args.compute_density else "input",
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "timing": "frames timed without per-stage events; stage times from a separate pass"},
             "e2e": {"value": fr.n / e2e_step, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "fwd_bwd": fb,
+            "fwd_bwd": detail.get("fwd_bwd") if detail else None,
+            "stage_ms": detail["stage_ms"] if detail else None,
+            "pipeline_roofline": detail["pipeline_roofline"] if detail else None,
+            "fp32_pipe": detail["fp32_pipe"] if detail else None,
+            "fp32_peak_tflops": {"value": fp32, "source": "measured (fsr_measure_fp32_rate, FMA chains)"},
+            "plain_path": extra.get("plain1m"),
+            "aniso8m": extra.get("aniso8m"),
             "batched": batched,
-            "gpu_launches": int(st.n_kernel_launches) * args.steps,
-            "stage_ms": {n: round(float(v), 4) for n, v in zip(_native.STAGE_NAMES, stage)},
+            "gpu_launches": n_launch * args.steps,
             "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -588,6 +710,14 @@ def main():
     if pg:
         pg.barrier()
         pg.destroy_process_group()
+
+
+def ctypes_fp32_rate(device):
+    import ctypes
+    from fluidsurfacereconstructiongpu_gb300 import _native
+    v = ctypes.c_double(0.0)
+    _native.check(_native.lib.fsr_measure_fp32_rate(int(device), ctypes.byref(v)))
+    return float(v.value)
 
 
 if __name__ == "__main__":

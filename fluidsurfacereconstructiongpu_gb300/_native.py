@@ -48,6 +48,12 @@ class FrameHeader(ctypes.Structure):
                 ("particle_radius", c_f32), ("particle_mass", c_f32)]
 
 
+class PairCounts(ctypes.Structure):
+    _fields_ = [("smooth_candidates", c_u64), ("smooth_contributing", c_u64), ("cov_candidates", c_u64),
+                ("cov_contributing", c_u64), ("field_candidates", c_u64), ("field_contributing", c_u64),
+                ("color_candidates", c_u64), ("color_contributing", c_u64)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n_particles", c_u64), ("n_cells", c_u64), ("n_grid_vertices", c_u64),
                 ("n_surface_particles", c_u64), ("n_involved_particles", c_u64), ("n_band_vertices", c_u64),
@@ -118,6 +124,8 @@ def _load():
         "fsr_batch_mesh_device": (ctypes.c_int, [c_vp, c_u32, P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_batch_copy_mesh": (ctypes.c_int, [c_vp, c_u32, c_vp, c_vp, c_u64, P(c_u64)]),
         "fsr_debug_fetch": (ctypes.c_int, [c_vp, c_u32, c_vp, c_u64, P(c_u64)]),
+        "fsr_count_pairs": (ctypes.c_int, [c_vp, P(PairCounts), c_vp]),
+        "fsr_measure_fp32_rate": (ctypes.c_int, [ctypes.c_int, P(ctypes.c_double)]),
         "fsr_read_xyz": (ctypes.c_int, [ctypes.c_char_p, P(FrameHeader), P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_free_host": (None, [c_vp]),
         "fsr_write_obj": (ctypes.c_int, [ctypes.c_char_p, c_vp, c_vp, c_u64]),

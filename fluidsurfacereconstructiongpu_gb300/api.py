@@ -197,6 +197,15 @@ class Reconstructor:
         N.check(N.lib.fsr_mesh_device(self._h, ctypes.byref(p), ctypes.byref(q), ctypes.byref(nv)), self._h)
         return p.value, q.value, nv.value
 
+    def pair_counts(self, stream=None) -> dict:
+        """Candidate and contributing pairs of the last frame's neighbour-sum
+        stages (fsr_count_pairs); synchronises the stream."""
+        import torch
+        pc = N.PairCounts()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        N.check(N.lib.fsr_count_pairs(self._h, ctypes.byref(pc), ctypes.c_void_p(s.cuda_stream)), self._h)
+        return {name: int(getattr(pc, name)) for name, _ in N.PairCounts._fields_}
+
     def stats(self) -> N.Stats:
         s = N.Stats()
         N.check(N.lib.fsr_get_stats(self._h, ctypes.byref(s)), self._h)

@@ -125,6 +125,7 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
         ca.sp = sp;
         ca.sorted = (const float4*)h->sorted.ptr;
         ca.mean = (const float4*)h->mean.ptr;
+        ca.mean32 = (const float4*)h->mean32.ptr;
         ca.smoothed = (const float4*)h->smoothed.ptr;
         ca.crec = (float4*)h->covrec.ptr;
         ca.ranges = (const uint2*)h->ranges.ptr;

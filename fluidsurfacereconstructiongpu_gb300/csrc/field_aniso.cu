@@ -629,9 +629,9 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                         1.0f / a.sc.cs, lane, pl, ph);  // psum is zeroed below
             // two sums per vertex: the involved particles' terms, then the
             // non-involved particles' (the unscaled kernel: about 1e-7 each,
-            // thousands of them), added among themselves and joined at the
-            // end, so that FP32 rounding does not drop or inflate them against
-            // a sum of order 1
+            // thousands of them) and the rounding errors of the first sum,
+            // added among themselves and joined at the end, so that FP32
+            // rounding does not drop or inflate them against a sum of order 1
             // the sums live in the warp's shared slice, so that the tile loops
             // need not be unrolled (the kernel's code stays small enough for
             // the instruction cache)
@@ -669,7 +669,13 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                             const uint32_t v = 32 * t + lane;
                             if (m && v < nv) {
                                 const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
-                                float s = w.psum[t][lane];
+                                // the chunk's terms are summed on their own and
+                                // then added to the vertex's sum with the
+                                // rounding error of that addition (two-sum)
+                                // kept in the second sum: with tens of
+                                // thousands of neighbours one running FP32 sum
+                                // drifts by more than 1e-5 of the field
+                                float s = 0.f;
                                 // two kept candidates per step, evaluated without
                                 // branches; their terms enter the sum in order
                                 for (uint32_t mm = m; mm;) {
@@ -684,7 +690,11 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                                     if (ina) s = fmaf(ca, ua, s);
                                     if (two && inb) s = fmaf(cb, ub, s);
                                 }
-                                w.psum[t][lane] = s;
+                                const float a0 = w.psum[t][lane];
+                                const float t0 = a0 + s;
+                                const float bp = t0 - a0;
+                                w.psum[t][lane] = t0;
+                                w.usum[t][lane] += (a0 - (t0 - bp)) + (s - bp);
                             }
                         }
                     }
@@ -706,7 +716,7 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                     const uint32_t v = 32 * t + lane;
                     if ((uint32_t)t < ntiles && v < nv) {
                         const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
-                        w.usum[t][lane] = unscaled_sum(w.mom, vp.x - ox, vp.y - oy, vp.z - oz);
+                        w.usum[t][lane] += unscaled_sum(w.mom, vp.x - ox, vp.y - oy, vp.z - oz);
                     }
                 }
             }
@@ -726,7 +736,7 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                     const uint32_t v = 32 * t + lane;
                     if ((uint32_t)t < ntiles && v < nv) {
                         const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
-                        float su = w.usum[t][lane];
+                        float su = 0.f;  // the chunk's terms, as for the involved candidates
                         uint32_t k = 0;
                         for (; k + 2 <= cnt; k += 2) {
                             const float4 qa = w.rec[k], qb = w.rec[k + 1];
@@ -745,7 +755,7 @@ __global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uin
                             const float ua = 1.0f - q2a;
                             if (q2a < 1.0f) su = fmaf(qa.w, ua * ua * ua, su);
                         }
-                        w.usum[t][lane] = su;
+                        w.usum[t][lane] += su;
                     }
                 }
                 __syncwarp();

@@ -63,7 +63,7 @@ struct fsr_handle {
     fsr::DevBuf keys0, vals0, keys1, vals1, radix_tmp;
     fsr::DevBuf sorted;                  // float4 x,y,z,density in cell order
     fsr::DevBuf psurf;                   // Akinci12 per-particle surface flags
-    fsr::DevBuf mean, smoothed, grec, qrec;  // Yu13
+    fsr::DevBuf mean, mean32, smoothed, grec, qrec;  // Yu13 (mean: compensated; mean32: the reference's FP32 mean)
     fsr::DevBuf covrec;                  // Yu13: normalised covariance, weight sum, neighbour-count flag
     fsr::DevBuf pflags;                  // u32 surface flags (debug)
     fsr::DevBuf rho;                     // computed densities, sorted order (FSR_FLAG_COMPUTE_DENSITY)

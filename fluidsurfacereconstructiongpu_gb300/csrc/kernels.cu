@@ -450,14 +450,24 @@ __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src,
 }
 
 // ------------------------------------------------------------ anisotropic path
-// calculationOfMeanAndSmoothParticles (cu:598-658).  The mean decides the
-// neighbour counts of the covariance stage, so it is summed in the
-// reference's order with the reference's roundings.  smoothed.w = m / rho.
+// calculationOfMeanAndSmoothParticles (cu:598-658).  Two means per particle:
+// * mean32: the reference's FP32 sum sum(w x) / sum(w) in its order with its
+//   roundings.  It decides the neighbour counts of the covariance stage, so
+//   it must be the reference's bit for bit.
+// * mean: the same quantity to near FP64 accuracy, as x_i + sum(w (x_j -
+//   x_i)) / sum(w).  The offsets x_j - x_i are exact (Sterbenz) and at most R
+//   long, so their sums stay small; they are summed per staged chunk (or
+//   cell row) and the chunk sums, like the weights, are added with Kahan
+//   compensation.  The reference's own FP32 sum of absolute coordinates is
+//   off by up to 4.5e-7 (1M-particle frame) and by more with thousands of
+//   neighbours; the covariance is taken about this mean, and the smoothed
+//   positions are formed from it.  mean.w = its weight sum (the adjoint
+//   divides by it); smoothed.w = m / rho.
 __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
                                                      float R_rcp, float R_lt2, int coop_ok, float one_minus_lambda,
                                                      float lambda, float mass, float4* __restrict__ mean,
-                                                     float4* __restrict__ smoothed)
+                                                     float4* __restrict__ mean32, float4* __restrict__ smoothed)
 {
     __shared__ float4 s_q[kThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -472,8 +482,12 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
                                    cell1(p.z, sp.min[2], sp.cs), 2, sp),
                             p.x, p.y, p.z, cull_radius(R, sp.cs), sp);
     float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+    // chunk sums of w and w (x_j - x_i), and their compensated totals
+    float cw = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    Kahan tw, tx, ty, tz;
     auto add = [&](const float4& q) {
-        const float d2 = dot3_rn(__fsub_rn(p.x, q.x), __fsub_rn(p.y, q.y), __fsub_rn(p.z, q.z));
+        const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y), dz = __fsub_rn(p.z, q.z);
+        const float d2 = dot3_rn(dx, dy, dz);
         if (!(d2 < R_lt2)) return;  // d >= R: weight 0, and +0 terms leave the sums unchanged
         const float s = div_exact(__fsqrt_rn(d2), R, R_rcp);
         const float wt = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(s, s), s));
@@ -481,6 +495,17 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
         mx = __fadd_rn(mx, __fmul_rn(q.x, wt));
         my = __fadd_rn(my, __fmul_rn(q.y, wt));
         mz = __fadd_rn(mz, __fmul_rn(q.z, wt));
+        cw = __fadd_rn(cw, wt);
+        cx = __fmaf_rn(-wt, dx, cx);
+        cy = __fmaf_rn(-wt, dy, cy);
+        cz = __fmaf_rn(-wt, dz, cz);
+    };
+    auto fold = [&]() {
+        tw.add(cw);
+        tx.add(cx);
+        ty.add(cy);
+        tz.add(cz);
+        cw = cx = cy = cz = 0.f;
     };
     auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
         const uint32_t c0 = lin3(x0, yy, zz, sp);
@@ -521,6 +546,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
                     const uint32_t cnt = stage_in_box(sorted, base, end, box, sq, lane);
                     __syncwarp();
                     for (uint32_t k = 0; k < cnt; ++k) add(sq[k]);
+                    fold();
                     __syncwarp();
                 }
             }
@@ -531,6 +557,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
                 uint32_t beg, end;
                 row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
                 for (uint32_t i = beg; i < end; ++i) add(__ldg(&sorted[i]));
+                fold();
             }
     }
     if (!active) return;
@@ -538,10 +565,13 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
     mx = __fdiv_rn(mx, ws);
     my = __fdiv_rn(my, ws);
     mz = __fdiv_rn(mz, ws);
-    mean[t] = make_float4(mx, my, mz, ws);  // w: the weight sum (the adjoint divides by it)
-    smoothed[t] = make_float4(__fadd_rn(__fmul_rn(one_minus_lambda, p.x), __fmul_rn(lambda, mx)),
-                              __fadd_rn(__fmul_rn(one_minus_lambda, p.y), __fmul_rn(lambda, my)),
-                              __fadd_rn(__fmul_rn(one_minus_lambda, p.z), __fmul_rn(lambda, mz)),
+    mean32[t] = make_float4(mx, my, mz, ws);
+    const float W = tw.s - tw.c;
+    const float ax = p.x + (tx.s - tx.c) / W, ay = p.y + (ty.s - ty.c) / W, az = p.z + (tz.s - tz.c) / W;
+    mean[t] = make_float4(ax, ay, az, W);  // w: the weight sum (the adjoint divides by it)
+    smoothed[t] = make_float4(__fadd_rn(__fmul_rn(one_minus_lambda, p.x), __fmul_rn(lambda, ax)),
+                              __fadd_rn(__fmul_rn(one_minus_lambda, p.y), __fmul_rn(lambda, ay)),
+                              __fadd_rn(__fmul_rn(one_minus_lambda, p.z), __fmul_rn(lambda, az)),
                               __fdiv_rn(mass, p.w));
 }
 
@@ -556,8 +586,11 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
 // a small block gives its registers back as soon as its two warps are done,
 // so the working warps' blocks fill the SM.
 constexpr int kCovThreads = 64;
+#ifndef FSR_COV_MIN_BLOCKS
+#define FSR_COV_MIN_BLOCKS 16
+#endif
 
-__global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ctr)
+__global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs a, Counters* ctr)
 {
     __shared__ float4 s_q[kCovThreads];  // 32 staged candidates per warp
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -567,26 +600,45 @@ __global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ct
     const int lane = threadIdx.x & 31;
     float4* sq = s_q + (threadIdx.x & ~31u);
     const float4 p = act ? a.sorted[t] : make_float4(0.f, 0.f, 0.f, 1.f);
+    // m: the compensated mean the covariance is taken about; m32: the
+    // reference's FP32 mean, which decides the neighbour count (dist <= r,
+    // cu:746).  They differ by the FP32 mean's rounding error, dm.
     const float4 m = act ? a.mean[t] : p;
+    float dm;
+    {
+        const float4 m32 = act ? a.mean32[t] : p;
+        dm = sqrtf(fmaf(m.x - m32.x, m.x - m32.x, fmaf(m.y - m32.y, m.y - m32.y, (m.z - m32.z) * (m.z - m32.z))));
+    }
+    const float cr = cull_radius(a.R, a.sp.cs) + 2.0f * dm;
+    // a candidate within R of either mean lies within R + dm of m
+    const float pre2 = (a.R * 1.0001f + 2.0f * dm) * (a.R * 1.0001f + 2.0f * dm);
+    // |q - m|^2 below in2 (above out2) puts q within (beyond) R of m32 with a
+    // margin far above the roundings of both squared distances: only
+    // candidates in the shell between them take the reference's test
+    const float rin = (a.R - dm) * (1.0f - 1e-5f), rout = (a.R + dm) * (1.0f + 1e-5f);
+    const float in2 = rin > 0.f ? rin * rin : 0.f, out2 = rout * rout;
     // the window is centred on the particle's cell (cu:710-716); only
-    // particles within R of the mean count or weigh, so cells beyond R of the
-    // mean on some axis are skipped
+    // particles within R of the means count or weigh, so cells beyond R of
+    // them on some axis are skipped
     const Window w = narrow(window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
                                    cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp),
-                            m.x, m.y, m.z, cull_radius(a.R, a.sp.cs), a.sp);
+                            m.x, m.y, m.z, cr, a.sp);
     CovAccum acc;
     uint32_t nn = 0;
     // d > R: neither counted nor weighed
     auto take = [&](const float4& q) {
         const float vx = __fsub_rn(q.x, m.x), vy = __fsub_rn(q.y, m.y), vz = __fsub_rn(q.z, m.z);
         const float d2 = dot3_rn(vx, vy, vz);
-        if (d2 < a.R_le2) {
+        if (d2 < in2) {
             ++nn;
-            if (d2 < a.R_lt2) acc.add(vx, vy, vz, div_exact(__fsqrt_rn(d2), a.R, a.R_rcp));
+        } else if (d2 < out2) {  // rare: m32 is loaded again (L1) rather than kept in registers
+            const float4 m32 = a.mean32[t];
+            if (dot3_rn(__fsub_rn(q.x, m32.x), __fsub_rn(q.y, m32.y), __fsub_rn(q.z, m32.z)) < a.R_le2) ++nn;
         }
+        if (d2 < a.R_lt2) acc.add(vx, vy, vz, div_exact(__fsqrt_rn(d2), a.R, a.R_rcp));
     };
-    auto dist2 = [&](const float4& q) {
-        return dot3_rn(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), __fsub_rn(q.z, m.z));
+    auto near = [&](const float4& q) {
+        return dot3_rn(__fsub_rn(q.x, m.x), __fsub_rn(q.y, m.y), __fsub_rn(q.z, m.z)) < pre2;
     };
     auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
         const uint32_t c0 = lin3(x0, yy, zz, a.sp);
@@ -615,7 +667,7 @@ __global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ct
     }
     if (compact) {
         // candidates beyond R of every lane's mean are dropped at staging
-        const WarpBox box = warp_box(act, m.x, m.y, m.z, cull_radius(a.R, a.sp.cs));
+        const WarpBox box = warp_box(act, m.x, m.y, m.z, cr);
         for (int zz = ulo[2]; zz <= uhi[2]; ++zz)
             for (int yy = ulo[1]; yy <= uhi[1]; ++yy) {
                 uint32_t beg, end;
@@ -626,8 +678,7 @@ __global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ct
                     uint32_t k = 0;
                     for (; k + 4 <= cnt; k += 4) {
                         const float4 q0 = sq[k], q1 = sq[k + 1], q2 = sq[k + 2], q3 = sq[k + 3];
-                        const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
-                        const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
+                        const bool n0 = near(q0), n1 = near(q1), n2 = near(q2), n3 = near(q3);
                         if (n0) take(q0);
                         if (n1) take(q1);
                         if (n2) take(q2);
@@ -649,8 +700,7 @@ __global__ void __launch_bounds__(kCovThreads, 16) k_cov(CovArgs a, Counters* ct
                 for (; i + 4 <= end; i += 4) {
                     const float4 q0 = __ldg(&a.sorted[i]), q1 = __ldg(&a.sorted[i + 1]);
                     const float4 q2 = __ldg(&a.sorted[i + 2]), q3 = __ldg(&a.sorted[i + 3]);
-                    const bool n0 = dist2(q0) < a.R_le2, n1 = dist2(q1) < a.R_le2;
-                    const bool n2 = dist2(q2) < a.R_le2, n3 = dist2(q3) < a.R_le2;
+                    const bool n0 = near(q0), n1 = near(q1), n2 = near(q2), n3 = near(q3);
                     if (n0) take(q0);
                     if (n1) take(q1);
                     if (n2) take(q2);
@@ -1074,7 +1124,7 @@ void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* 
 
 
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
-                   float R, float lambda, float mass, float4* mean, float4* smoothed)
+                   float R, float lambda, float mass, float4* mean, float4* mean32, float4* smoothed)
 {
     if (!n) return;
     // (1.0 - lambda) is evaluated in double and rounded (cu:656)
@@ -1083,7 +1133,8 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     // below two cells (see k_smooth)
     const int coop_ok = (R * 1.0001f + 1e-4f * sp.cs) < 2.0f * sp.cs * 0.9999f ? 1 : 0;
     k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, 1.0f / R, sqrt_threshold(R, false),
-                                                       coop_ok, oml, lambda, mass, mean, smoothed);
+                                                       coop_ok, oml, lambda, mass, mean, mean32,
+                                                       smoothed);
     ++g_launches;
 }
 

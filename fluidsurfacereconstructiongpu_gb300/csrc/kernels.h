@@ -76,9 +76,10 @@ struct IsoFieldArgs {
 void launch_field_iso_grouped(const KernelCtx& c, bool tc01, const IsoFieldArgs& a, const BandView& band,
                               uint32_t ratio, Counters* ctr);
 
-// Yu13 smoothing: mean (exact FP32) and smoothed position with m/rho in w.
+// Yu13 smoothing: the compensated mean (w: weight sum), the reference's FP32
+// mean (mean32, w: its weight sum) and the smoothed position with m/rho in w.
 void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const uint2* ranges, const Grid& sp,
-                   float R, float lambda, float mass, float4* mean, float4* smoothed);
+                   float R, float lambda, float mass, float4* mean, float4* mean32, float4* smoothed);
 
 // Smallest float x whose correctly rounded square root is >= R (> R when
 // strict): sqrt_rn(d2) < R <=> d2 < sqrt_threshold(R, false) and
@@ -88,7 +89,8 @@ float sqrt_threshold(float R, bool strict);
 struct CovArgs {
     Grid sp;
     const float4* sorted;
-    const float4* mean;
+    const float4* mean;      // compensated mean (the covariance's centre), w = weight sum
+    const float4* mean32;    // the reference's FP32 mean (the neighbour-count decision)
     const float4* smoothed;  // x,y,z smoothed, w = m / rho
     const uint2* ranges;
     const uint32_t* skeys;

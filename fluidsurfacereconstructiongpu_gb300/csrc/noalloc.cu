@@ -86,6 +86,9 @@ extern "C" fsr_status fsr_spatial_hash_noalloc(const fsr_frame_header* hdr, floa
 {
     using namespace fsr;
     if (!hdr || !n_cells) return FSR_ERR_INVALID_ARGUMENT;
+    // an error left pending by earlier work on this thread is not this
+    // call's: report it without consuming it, and queue nothing
+    if (cudaPeekAtLastError() != cudaSuccess) return FSR_ERR_CUDA;
     if (n > kMax) return FSR_ERR_TOO_LARGE;  // beyond the static scratch
     if (n > 0 && (!d_xyz || !d_density || !d_sorted_xyz || !d_sorted_density)) return FSR_ERR_INVALID_ARGUMENT;
     fsr_params p{};

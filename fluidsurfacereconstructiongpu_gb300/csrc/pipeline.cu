@@ -175,7 +175,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &gflag, &glist, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &valid,   &mean,   &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &valid,   &mean,   &mean32, &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
 }
 
 // ------------------------------------------------------------ frame
@@ -236,6 +236,7 @@ fsr_status frame_buffers(fsr_handle* h, const FramePlan& fp)
         CK(h->invol.ensure(C));
         CK(h->cell_rmax.ensure(4ull * C));
         CK(h->mean.ensure(16ull * nn));
+        CK(h->mean32.ensure(16ull * nn));
         CK(h->smoothed.ensure(16ull * nn));
         CK(h->grec.ensure(64ull * nn));
         CK(h->qrec.ensure(48ull * nn));
@@ -357,12 +358,13 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     if (yu13) {
         const float R = h_r * p.aniso_radius_over_h;
         launch_smooth(kc, sorted, n, ranges, sp, R, p.smoothing_lambda, hdr.particle_mass, (float4*)h->mean.ptr,
-                      (float4*)h->smoothed.ptr);
+                      (float4*)h->mean32.ptr, (float4*)h->smoothed.ptr);
         mark(5);
         CovArgs ca{};
         ca.sp = sp;
         ca.sorted = sorted;
         ca.mean = (const float4*)h->mean.ptr;
+        ca.mean32 = (const float4*)h->mean32.ptr;
         ca.smoothed = (const float4*)h->smoothed.ptr;
         ca.ranges = ranges;
         ca.skeys = skeys;
@@ -804,7 +806,7 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
         for (uint64_t i = 0; i < n; ++i) ((float*)dst)[i] = tmp[4 * i + 3];
         break;
     }
-    case FSR_DBG_MEAN: CK(copy4(h->mean, 4, 3, n, (float*)dst)); break;
+    case FSR_DBG_MEAN: CK(copy4(h->mean32, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_SMOOTHED: CK(copy4(h->smoothed, 4, 3, n, (float*)dst)); break;
     case FSR_DBG_G: {
         std::vector<float> tmp(16 * n);

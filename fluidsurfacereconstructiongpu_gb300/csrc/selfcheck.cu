@@ -1,6 +1,7 @@
 // Device self-checks of arithmetic shortcuts against CUDA's own operations.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -97,5 +98,64 @@ extern "C" fsr_status fsr_check_division(float b, uint64_t* n_checked, uint64_t*
     if (e != cudaSuccess) return FSR_ERR_CUDA;
     *n_checked = (uint64_t)hi_bits + 1;
     *n_mismatch = out[0];
+    return FSR_OK;
+}
+
+namespace {
+
+// Independent FMA chains per thread: the FP32 pipe's issue rate, not its
+// latency, bounds the kernel.  The result is stored only when it is 0 (it
+// never is for these inputs) so that the chains are not removed.
+__global__ void __launch_bounds__(256) k_fma_rate(float a, float b, int iters, float* sink)
+{
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = (float)(threadIdx.x + k) * 1e-3f + 1.0f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += x[k];
+    if (s == 0.0f) *sink = s;
+}
+
+}  // namespace
+
+extern "C" fsr_status fsr_measure_fp32_rate(int device, double* tflops)
+{
+    if (!tflops) return FSR_ERR_INVALID_ARGUMENT;
+    *tflops = 0.0;
+    if (cudaSetDevice(device) != cudaSuccess) return FSR_ERR_CUDA;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    float* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) return FSR_ERR_OUT_OF_MEMORY;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const unsigned blocks = (unsigned)sms * 8;  // 8 blocks of 256 threads per SM: every warp slot busy
+    const int iters = 4096;
+    double best = 0.0;
+    // the multiplier keeps every chain bounded: x -> x a + b with |a| < 1
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        k_fma_rate<<<blocks, 256>>>(0.999f, 1e-3f, iters, sink);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * 8 * 16 * (double)iters * 256.0 * blocks;
+        if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    const cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return FSR_ERR_CUDA;
+    *tflops = best;
     return FSR_OK;
 }

@@ -202,7 +202,7 @@ typedef enum fsr_debug_array {
     FSR_DBG_FIELD = 6,           /* f32[B]  field at the band vertices */
     FSR_DBG_MC_INFO = 7,         /* u32[B]  case | nverts << 8 | valid << 16 */
     FSR_DBG_VALID_CUBES = 8,     /* u32[Q]  positions in the band list of valid cubes */
-    FSR_DBG_MEAN = 9,            /* f32[N*3] Yu13 weighted means (sorted order) */
+    FSR_DBG_MEAN = 9,            /* f32[N*3] Yu13 weighted means, the reference's FP32 sums (sorted order) */
     FSR_DBG_SMOOTHED = 10,       /* f32[N*3] Yu13 smoothed positions */
     FSR_DBG_G = 11,              /* f32[N*9] Yu13 G matrices, row-major, sorted order (*) */
     FSR_DBG_WELD_KEYS = 12,      /* u64[3T] grid edge of each soup vertex, 3 x lower end point + axis
@@ -212,6 +212,27 @@ typedef enum fsr_debug_array {
 
 fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t dst_bytes,
                            uint64_t* bytes_needed);
+
+/* Pair counts of the last frame's neighbour-sum stages, for throughput
+ * accounting (a diagnostic; the reference has none).  For each stage: the
+ * candidate pairs the reference's loops visit, i.e. every particle of the
+ * unit's cell window (calculationOfMeanAndSmoothParticles,
+ * ReconstructionCUDA.cu:598-658, and calculationOfTransformMatricesFor-
+ * Particles, cu:689-827: +-2 cells per particle; computationOfScalarFieldGrid,
+ * cu:830-906: +-2 cells per band vertex; updateScalarFieldValueZB05 / TC01,
+ * cu:178-289, and extractionOfSurfaceParticlesUsingColorField, cu:909-971:
+ * +-1 cells), and of those the pairs inside the kernel's support, whose
+ * terms are non-zero.  Counted by separate brute-force kernels over the
+ * frame's buffers (the frame's own kernels skip most non-contributing
+ * candidates); synchronises `stream`.  Stages the method does not run are 0. */
+typedef struct fsr_pair_counts {
+    uint64_t smooth_candidates, smooth_contributing;  /* Yu13 smoothing: d < R */
+    uint64_t cov_candidates, cov_contributing;        /* Yu13 covariance, involved particles: |x - mean| < R */
+    uint64_t field_candidates, field_contributing;    /* field: |G (x~ - v)| < 1 (Yu13), d < h (ZB05, TC01) */
+    uint64_t color_candidates, color_contributing;    /* Akinci12 colour field: 0 < d < h */
+} fsr_pair_counts;
+
+fsr_status fsr_count_pairs(fsr_handle* h, fsr_pair_counts* out, void* stream);
 
 /* ---- spatial hashing without allocation ------------------------------
  *
@@ -238,10 +259,14 @@ fsr_status fsr_debug_fetch(fsr_handle* h, uint32_t which, void* dst, uint64_t ds
  * that loads the library holds on each device it uses until it exits; larger
  * n is rejected with FSR_ERR_TOO_LARGE before any GPU work.  The first call
  * on a device looks up that array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  All calls on a device
- * share the array: calls whose GPU work overlaps (two streams, two host
- * threads) race and corrupt each other's results.  It calls no cudaMalloc or
- * cudaFree; the work is queued on `stream` and nothing is synchronised. */
+ * make that first call before any stream capture.  The address is kept for
+ * the life of the process, so a device reset (cudaDeviceReset) between calls
+ * is not supported.  All calls on a device share the array: calls whose GPU
+ * work overlaps (two streams, two host threads) race and corrupt each
+ * other's results.  A CUDA error already pending on the calling thread makes
+ * the call return FSR_ERR_CUDA at once, leaving that error pending.  It calls
+ * no cudaMalloc or cudaFree; the work is queued on `stream` and nothing is
+ * synchronised. */
 #define FSR_NOALLOC_MAX_PARTICLES (1u << 18)
 
 fsr_status fsr_spatial_hash_noalloc(const fsr_frame_header* hdr, float cell_size_scale,
@@ -331,6 +356,12 @@ fsr_status fsr_check_division(float R, uint64_t* n_checked, uint64_t* n_mismatch
  * it and the double expression for every float x in (0, 1] and counts the
  * results that differ (0 expected). */
 fsr_status fsr_check_spiky_grad(double k, uint64_t* n_checked, uint64_t* n_mismatch);
+
+/* Measured FP32 FMA rate of `device` in TFLOP/s (2 flops per FMA; a kernel of
+ * independent FMA chains on every warp slot, best of three timed launches):
+ * the denominator of the pair kernels' FP32-pipe fractions.  No counterpart
+ * in the reference. */
+fsr_status fsr_measure_fp32_rate(int device, double* tflops);
 
 /* ---- file formats -------------------------------------------------- */
 

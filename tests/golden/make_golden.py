@@ -18,6 +18,7 @@ import hashlib
 import json
 import os
 import re
+import subprocess
 import sys
 
 import numpy as np
@@ -29,7 +30,9 @@ sys.path.insert(0, ROOT)
 from fluidsurfacereconstructiongpu_gb300 import synthetic  # noqa: E402
 from oracle import pipeline as P  # noqa: E402
 
-REF_ROOT = os.environ.get("REF_ROOT", "/root/reference")
+# the reference checkout, as the oracle's build recipe resolves it (REF_ROOT)
+REF_ROOT = subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), "--print-root"],
+                          capture_output=True, text=True, check=True).stdout.strip()
 
 CASES = [
     # name, method, frame factory, extra params

@@ -8,7 +8,9 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("REF_ROOT", "/root/reference")
+# the reference checkout, as the oracle's build recipe resolves it (REF_ROOT)
+REF = subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh"), "--print-root"], capture_output=True,
+                     text=True, check=True).stdout.strip()
 SRC = os.path.join(REF, "FluidSurfaceReconstruction")
 FILES = ["main.cpp"] + ["GPU/" + f for f in ("ReconstructorGPU.cpp", "ReconstructorGPUOurs.cpp",
                                              "ReconstructorGPUOursZB05.cpp", "ReconstructorGPUOursYu13.cpp",

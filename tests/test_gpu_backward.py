@@ -156,3 +156,33 @@ def test_autograd_function():
     g_ref = rec.backward(torch.from_numpy(_grad_mesh(pos.detach().cpu().numpy()).astype(np.float32)).cuda())
     assert torch.allclose(xyz.grad, g_ref, rtol=1e-4, atol=1e-9)
     rec.close()
+
+
+@pytest.mark.parametrize("method", ["zb05", "akinci"])
+def test_autograd_radius_gradient(method):
+    """The autograd wrapper returns dL/d(particle radius) for the fields that
+    use it, equal to the C ABI's, and the radius tensor's value is the one
+    the frame is reconstructed with."""
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api, synthetic
+    from fluidsurfacereconstructiongpu_gb300.autograd import reconstruct_surface
+    fr = synthetic.lattice_cube(10, 0.0125, seed=2, origin=(0.3, 0.3, 0.3))
+    rec = api.Reconstructor(method, 0)
+    xyz = torch.from_numpy(fr.pos).cuda().requires_grad_(True)
+    den = torch.from_numpy(fr.density).cuda()
+    r = torch.tensor(fr.particle_radius * 1.05, dtype=torch.float32, device="cuda", requires_grad=True)
+    pos = reconstruct_surface(xyz, den, rec, api.header_of(fr), radius=r)
+    c = torch.tensor(C0, dtype=torch.float32, device="cuda")
+    loss = ((pos - c).norm(dim=1) - R0).pow(2).mean()
+    loss.backward()
+    hdr = api.header_of(fr)
+    hdr.particle_radius = float(r.item())
+    rec.reconstruct(xyz.detach(), den, hdr)
+    pos2, _ = rec.mesh_tensors()
+    assert torch.equal(pos.detach(), pos2)
+    g_ref, gr_ref = rec.backward(torch.from_numpy(_grad_mesh(pos2.cpu().numpy()).astype(np.float32)).cuda(),
+                                 with_radius=True)
+    assert gr_ref != 0.0
+    assert abs(float(r.grad) - gr_ref) <= 1e-4 * abs(gr_ref)
+    assert torch.allclose(xyz.grad, g_ref, rtol=1e-4, atol=1e-9)
+    rec.close()

@@ -101,3 +101,55 @@ def test_noalloc_rejects_oversize_and_small_range_buffers():
     st = f(ctypes.byref(hdr), ctypes.c_float(1.0), x.data_ptr(), d.data_ptr(), fr.n, x.data_ptr(), d.data_ptr(),
            x.data_ptr(), 1, None, None, ctypes.byref(ncells), None)
     assert st == 7 and ncells.value > 1  # FSR_ERR_CAPACITY, nothing written
+
+
+def _call(N, f, fr, pos, cap, with_optional=True):
+    """One call on the given positions; returns status, n_cells, perm, ranges,
+    sorted xyz and the out-of-grid count (None when not requested)."""
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api
+    n = pos.shape[0]
+    xyz = torch.from_numpy(np.ascontiguousarray(pos, np.float32)).cuda()
+    den = torch.full((n,), 1000.0, device="cuda")
+    out_xyz = torch.full((max(n, 1), 3), -1.0, device="cuda")
+    out_den = torch.full((max(n, 1),), -1.0, device="cuda")
+    ranges = torch.zeros((cap, 2), dtype=torch.int32, device="cuda")
+    perm = torch.full((max(n, 1),), -1, dtype=torch.int32, device="cuda")
+    oog = torch.full((1,), 7, dtype=torch.int32, device="cuda")
+    ncells = ctypes.c_uint64(0)
+    st = f(ctypes.byref(api.header_of(fr)), ctypes.c_float(1.0), xyz.data_ptr() if n else None,
+           den.data_ptr() if n else None, n, out_xyz.data_ptr() if n else None, out_den.data_ptr() if n else None,
+           ranges.data_ptr(), cap, perm.data_ptr() if with_optional else None,
+           oog.data_ptr() if with_optional else None, ctypes.byref(ncells),
+           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    c = int(ncells.value)
+    return (st, c, perm[:n].cpu().numpy().view(np.uint32), ranges[:c].cpu().numpy().view(np.uint32),
+            out_xyz[:n].cpu().numpy(), int(oog.item()) if with_optional else None)
+
+
+def test_noalloc_edge_cases():
+    """n = 0 and n = 1, a particle outside the grid (counted, no write out of
+    bounds: it is hashed to cell 0) and null optional outputs."""
+    N, f = _bind()
+    fr = _frame(8, seed=1, origin=(0.3, 0.3, 0.3))
+    cap = 64 ** 3
+    st, c, _, ranges, _, oog = _call(N, f, fr, np.zeros((0, 3), np.float32), cap)
+    assert st == N.FSR_OK and c > 0 and oog == 0
+    assert np.all(ranges == 0xFFFFFFFF)
+    one = fr.pos[5:6]
+    st, c, perm, ranges, xyz, oog = _call(N, f, fr, one, cap)
+    assert st == N.FSR_OK and oog == 0 and perm.tolist() == [0]
+    assert np.array_equal(xyz, one)
+    nonempty = np.flatnonzero(ranges[:, 0] != 0xFFFFFFFF)
+    assert nonempty.size == 1 and ranges[nonempty[0]].tolist() == [0, 1]
+    pos = fr.pos.copy()
+    pos[3] = [5.0, 0.5, 0.5]
+    st, _, perm, ranges, _, oog = _call(N, f, fr, pos, cap)
+    assert st == N.FSR_OK and oog == 1
+    assert sorted(perm.tolist()) == list(range(fr.n))
+    # without the optional outputs the sorted particles and ranges are the same
+    st1, _, _, r1, x1, _ = _call(N, f, fr, fr.pos, cap)
+    st2, _, _, r2, x2, none = _call(N, f, fr, fr.pos, cap, with_optional=False)
+    assert st1 == st2 == N.FSR_OK and none is None
+    assert np.array_equal(r1, r2) and np.array_equal(x1, x2)
