@@ -230,7 +230,8 @@ def run_batch_leg(dev, stream, steps, warmup, flush, cfg=BATCH):
             "methods": {m: sum(1 for q, _ in frames if q == m) for m in cfg["methods"]},
             "value": total / (tb / 1e3), "ms_per_step": tb, "single_frame_value": total / (ts / 1e3),
             "single_frame_ms": ts, "speedup_vs_single_frame": ts / tb, "lanes": int(tun.lanes),
-            "grid_div": int(tun.grid_div), "autotune_candidates": int(tun.n_candidates),
+            "grid_div": int(tun.grid_div), "block_threads": int(tun.block_threads),
+            "autotune_candidates": int(tun.n_candidates),
             "gpu_launches_per_step": launches,
             "note": "step = one fsr_reconstruct_batch call (inputs copied device-to-device, one graph launch, "
                     "one synchronisation); single frame = the same frames through fsr_reconstruct one by one"}
@@ -394,6 +395,39 @@ def run_io_leg(args, w):
         shutil.rmtree(d, ignore_errors=True)
 
 
+def reference_gpu_leg(workloads, steps, warmup):
+    """The reference's own CUDA kernels on this GPU (its ReconstructionCUDA.cu
+    built for sm_103a as a cubin, oracle/ref_gpu), driven through its
+    kernel-level ABI in its frame order with its synchronisation after every
+    launch (oracle/ref_gpu/flow.py).  Timed over the reference's timer scope
+    (ReconstructorGPU.cpp:46-54): spatial hashing + the frame's stages."""
+    from oracle.ref_gpu import flow
+    if not flow.available("reference"):
+        return {"unavailable": "the reference's kernels were not built (no reference sources where build() ran)"}
+    L = flow.launchers("reference")
+    flow.bind_tables(L)
+    out = {"kind": "reference CUDA kernels (sm_103a cubin of its ReconstructionCUDA.cu) under a host "
+                   "restatement of its frame loop; FMA contraction as nvcc's default",
+           "steps": steps, "warmup": warmup}
+    for name in workloads:
+        w = WORKLOADS[name]
+        fr = make_frame(w)
+        prm = oracle_params(w, fr)
+        for _ in range(warmup):
+            flow.frame(L, w["method"], fr, prm, outputs=False)
+        ts = []
+        res = None
+        for _ in range(steps):
+            res, dt = flow.frame(L, w["method"], fr, prm, outputs=False)
+            ts.append(dt)
+        err = L.last_error()
+        t = float(np.mean(ts))
+        out[name] = {"ms_per_frame": t * 1e3, "value": fr.n / t, "unit": "particles/s",
+                     "band_vertices": int(res["n_band"]), "triangles": int(res.get("n_mesh_vertices", 0)) // 3,
+                     "launcher_error": err or None}
+    return out
+
+
 def pipeline_bytes(method, n, C, V, B, I, Q, T):
     """Algorithmic compulsory bytes of one forward frame and of its backward
     pass: every input read once, every output written once, every
@@ -533,6 +567,8 @@ def main():
     ap.add_argument("--no-backward", action="store_true", help="skip the forward+backward leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frames legs")
     ap.add_argument("--no-extra", action="store_true", help="skip the plain-path and 8M legs")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the GPU baseline of the reference's own kernels")
     ap.add_argument("--compute-density", action="store_true",
                     help="frames without densities: the GPU computes them (FSR_FLAG_COMPUTE_DENSITY); "
                          "no backward or batch legs")
@@ -591,6 +627,14 @@ def main():
         s, label, threads, sample = cpu_frame(w, fr)
         cpu = {"value": fr.n / s, "unit": "particles/s", "cores": threads, "kind": label, "sample": sample,
                "ms_per_frame": s * 1e3}
+
+    # the reference's own CUDA kernels on this GPU (rank 0, N = 1)
+    ref_gpu = None
+    if rank == 0 and world == 1 and not args.no_reference_gpu and args.workload == "aniso1m" and \
+            not args.compute_density:
+        ref_gpu = reference_gpu_leg(("aniso1m", "plain1m"), min(args.steps, 5), 1)
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
 
     rec = api.Reconstructor(w["method"], local, compute_density=args.compute_density, **recon_kwargs(w))
     hdr = api.header_of(fr)
@@ -703,7 +747,7 @@ def main():
             "aniso8m": extra.get("aniso8m"),
             "batched": batched,
             "gpu_launches": n_launch * args.steps,
-            "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu}
+            "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu, "reference_gpu": ref_gpu}
     if rank == 0:
         print(json.dumps(line), flush=True)
     rec.close()

@@ -77,7 +77,7 @@ class BatchFrame(ctypes.Structure):
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("lanes", c_u32), ("grid_div", c_u32), ("n_candidates", c_u32), ("kernels_per_launch", c_u32),
-                ("graph_ms", c_f32), ("frames_ms", c_f32)]
+                ("graph_ms", c_f32), ("frames_ms", c_f32), ("block_threads", c_u32)]
 
 
 BATCH_RETUNE = 0x1

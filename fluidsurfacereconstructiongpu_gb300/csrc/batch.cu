@@ -8,8 +8,9 @@
 // longest-processing-time first, and the graph is captured: a fork event on
 // the origin stream, each lane waits on it and queues its frames' kernels
 // back to back, the origin joins every lane.  The autotuner captures and
-// times each (lanes, grid_div) candidate on the real frames and keeps the
-// fastest executable graph.
+// times each (lanes, grid_div) candidate on the real frames, then the best
+// one again with 128-thread blocks for the per-item and warp-staged kernels
+// (the block shape), and keeps the fastest executable graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -197,6 +198,7 @@ fsr_status size_frames(fsr_batch* b, cudaStream_t st)
     for (uint32_t i = 0; i < count; ++i) {
         fsr_handle* h = b->slots[i];
         h->grid_div = 1;
+        h->block = 256;
         bool retry = true;
         for (int attempt = 0; attempt < 4 && retry; ++attempt) {
             FK(b, i, frame_buffers(h, b->plans[i]));
@@ -222,13 +224,18 @@ fsr_status plan(fsr_batch* b, uint32_t flags, cudaStream_t st)
     fsr_status s = size_frames(b, st);
     if (s != FSR_OK) return s;
     const uint32_t count = (uint32_t)b->plans.size();
-    std::vector<std::pair<uint32_t, uint32_t>> cand;
+    // candidates: (lanes, grid_div, block) -- the block shape is tried for
+    // the best (lanes, grid_div) after those have been timed at 256 threads
+    struct Cand {
+        uint32_t lanes, grid_div, block;
+    };
+    std::vector<Cand> cand;
     if (flags & FSR_BATCH_NO_AUTOTUNE) {
-        cand.push_back({std::min<uint32_t>(count, 8), 1});
+        cand.push_back({std::min<uint32_t>(count, 8), 1, 256});
     } else {
         for (uint32_t L : {1u, 2u, 4u, 8u, 16u, 32u}) {
             if (L > count && L != 1) continue;
-            for (uint32_t gd : {1u, 4u}) cand.push_back({L, gd});
+            for (uint32_t gd : {1u, 4u}) cand.push_back({L, gd, 256});
         }
     }
     if (b->exec) {
@@ -237,18 +244,24 @@ fsr_status plan(fsr_batch* b, uint32_t flags, cudaStream_t st)
     }
     float best = 3.4e38f;
     uint32_t best_k = 0;
-    for (const auto& c : cand) {
-        for (auto h : b->slots) h->grid_div = (int)c.second;
-        const std::vector<uint32_t> lane_of = assign_lanes(b->cost_ms, c.first);
+    uint32_t n_timed = 0;
+    auto try_cand = [&](const Cand& c) -> fsr_status {
+        for (auto h : b->slots) {
+            h->grid_div = (int)c.grid_div;
+            h->block = (int)c.block;
+        }
+        const std::vector<uint32_t> lane_of = assign_lanes(b->cost_ms, c.lanes);
         cudaGraphExec_t ex = nullptr;
         uint32_t k = 0;
-        if ((s = capture(b, c.first, lane_of, &ex, &k)) != FSR_OK) return s;
+        fsr_status cs = capture(b, c.lanes, lane_of, &ex, &k);
+        if (cs != FSR_OK) return cs;
         float ms = 0.f;
+        ++n_timed;
         if (cand.size() > 1) {
-            s = time_exec(b, ex, st, 2, &ms);
-            if (s != FSR_OK) {
+            cs = time_exec(b, ex, st, 2, &ms);
+            if (cs != FSR_OK) {
                 cudaGraphExecDestroy(ex);
-                return s;
+                return cs;
             }
         }
         if (ms < best) {
@@ -257,14 +270,25 @@ fsr_status plan(fsr_batch* b, uint32_t flags, cudaStream_t st)
             best = ms;
             best_k = k;
             b->lane_of = lane_of;
-            b->tuning.lanes = c.first;
-            b->tuning.grid_div = c.second;
+            b->tuning.lanes = c.lanes;
+            b->tuning.grid_div = c.grid_div;
+            b->tuning.block_threads = c.block;
         } else {
             cudaGraphExecDestroy(ex);
         }
+        return FSR_OK;
+    };
+    for (const auto& c : cand)
+        if ((s = try_cand(c)) != FSR_OK) return s;
+    if (cand.size() > 1) {
+        const Cand c{b->tuning.lanes, b->tuning.grid_div, 128};
+        if ((s = try_cand(c)) != FSR_OK) return s;
     }
-    for (auto h : b->slots) h->grid_div = (int)b->tuning.grid_div;
-    b->tuning.n_candidates = (uint32_t)cand.size();
+    for (auto h : b->slots) {
+        h->grid_div = (int)b->tuning.grid_div;
+        h->block = (int)b->tuning.block_threads;
+    }
+    b->tuning.n_candidates = n_timed;
     b->tuning.kernels_per_launch = best_k;
     b->tuning.graph_ms = cand.size() > 1 ? best : 0.f;
     return FSR_OK;

@@ -85,6 +85,7 @@ struct fsr_handle {
 
     uint32_t cap_band = 0, cap_valid = 0, cap_mesh = 0;
     int grid_div = 1;                    // grid-stride kernels use num_sms * per_sm / grid_div blocks
+    int block = 256;                     // threads per block of the per-item and warp-staged kernels
     uint64_t launches_mark = 0;
     uint32_t launches_frame = 0;
     fsr::Counters* pinned_ctr = nullptr;

@@ -32,10 +32,17 @@ inline unsigned blocks_for(uint64_t n, int threads = kThreads)
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + threads - 1) / threads, 0x7fffffffULL));
 }
 
+// threads per block of the per-item and warp-staged kernels: the context's
+// block shape (a multiple of 32 up to kThreads, which their per-warp shared
+// arrays are sized for)
+inline int bs(const KernelCtx& c) { return (c.block >= 32 && c.block <= kThreads && c.block % 32 == 0) ? c.block : kThreads; }
+
 // grid for grid-stride kernels whose length is read on the device
 inline unsigned persistent_blocks(const KernelCtx& c, uint64_t cap, int per_sm = 8)
 {
-    const uint64_t want = (cap + kThreads - 1) / kThreads;
+    const uint64_t want = (cap + bs(c) - 1) / bs(c);
+    // per_sm counts blocks of kThreads threads: smaller blocks get proportionally more
+    per_sm = per_sm * (kThreads / bs(c));
     const uint64_t most = std::max<uint64_t>(1, (uint64_t)c.num_sms * per_sm / std::max(1, c.grid_div));
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, most));
 }
@@ -456,9 +463,11 @@ __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src,
 //   it must be the reference's bit for bit.
 // * mean: the same quantity to near FP64 accuracy, as x_i + sum(w (x_j -
 //   x_i)) / sum(w).  The offsets x_j - x_i are exact (Sterbenz) and at most R
-//   long, so their sums stay small; they are summed per staged chunk (or
-//   cell row) and the chunk sums, like the weights, are added with Kahan
-//   compensation.  The reference's own FP32 sum of absolute coordinates is
+//   long, so their sums stay small; they are summed per chunk of 32
+//   candidates and the chunk sums, like the weights, are added with Kahan
+//   compensation (neighbouring particles sum nearly the same candidates in
+//   the same order, so the rounding errors of long plain sums would be
+//   correlated between them and would not average out in the field).  The reference's own FP32 sum of absolute coordinates is
 //   off by up to 4.5e-7 (1M-particle frame) and by more with thousands of
 //   neighbours; the covariance is taken about this mean, and the smoothed
 //   positions are formed from it.  mean.w = its weight sum (the adjoint
@@ -556,7 +565,10 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
             for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
-                for (uint32_t i = beg; i < end; ++i) add(__ldg(&sorted[i]));
+                for (uint32_t i = beg; i < end; ++i) {
+                    add(__ldg(&sorted[i]));
+                    if (((i - beg) & 31u) == 31u) fold();  // chunks of 32, as in the staged walk
+                }
                 fold();
             }
     }
@@ -1046,7 +1058,7 @@ void launch_hash(const KernelCtx& c, const float* xyz, uint32_t n, const Grid& s
                  uint32_t* vals, Counters* ctr)
 {
     if (!n) return;
-    k_hash<<<blocks_for(n), kThreads, 0, c.stream>>>(xyz, n, sp, keys, vals, ctr);
+    k_hash<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(xyz, n, sp, keys, vals, ctr);
     ++g_launches;
 }
 
@@ -1054,7 +1066,7 @@ void launch_ranges_gather(const KernelCtx& c, const uint32_t* skeys, const uint3
                           const float* xyz, const float* dens, float4* sorted, uint2* ranges, uint8_t* occ)
 {
     if (!n) return;
-    k_ranges_gather<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, perm, n, xyz, dens, sorted, ranges, occ);
+    k_ranges_gather<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(skeys, perm, n, xyz, dens, sorted, ranges, occ);
     ++g_launches;
 }
 
@@ -1066,15 +1078,15 @@ void launch_density(const KernelCtx& c, float4* sorted, uint32_t n, const uint2*
     const float h2 = h * h;
     const float sigma = 315.0f / (64.0f * 3.1415926535898f);
     const float scale = mass * sigma / (h * h * h);
-    k_density<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, ext, h, h2, 1.0f / h2, scale, rho);
-    k_set_density<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, rho, n);
+    k_density<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(sorted, n, ranges, sp, ext, h, h2, 1.0f / h2, scale, rho);
+    k_set_density<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(sorted, rho, n);
     g_launches += 2;
 }
 
 void launch_surface_cells(const KernelCtx& c, const Grid& sp, const uint8_t* occ, uint8_t* surf)
 {
     const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
-    k_surface_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf);
+    k_surface_cells<<<blocks_for(C, bs(c)), bs(c), 0, c.stream>>>(sp, occ, surf);
     ++g_launches;
 }
 
@@ -1082,7 +1094,7 @@ void launch_involved_cells(const KernelCtx& c, const Grid& sp, const uint8_t* oc
                            uint8_t* invol)
 {
     const uint64_t C = (uint64_t)sp.res[0] * sp.res[1] * sp.res[2];
-    k_involved_cells<<<blocks_for(C), kThreads, 0, c.stream>>>(sp, occ, surf, invol);
+    k_involved_cells<<<blocks_for(C, bs(c)), bs(c), 0, c.stream>>>(sp, occ, surf, invol);
     ++g_launches;
 }
 
@@ -1100,7 +1112,7 @@ void launch_colorfield(const KernelCtx& c, const float4* sorted, uint32_t n, con
         khi = (float)K;
         klo = (float)(K - (double)khi);
     }
-    k_colorfield<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, skeys, sp, h, 1.0f / h,
+    k_colorfield<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(sorted, n, ranges, skeys, sp, h, 1.0f / h,
                                                            sqrt_threshold(h, false), k, khi, klo, mass, psurf);
     ++g_launches;
 }
@@ -1110,7 +1122,7 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
                        Counters* ctr)
 {
     if (!n) return;
-    k_band_stamp<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc,
+    k_band_stamp<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(sorted, skeys, surf, psurf, n, sc,
                                                            sqrt_threshold(thr, true), bits, ctr);
     ++g_launches;
 }
@@ -1118,7 +1130,7 @@ void launch_band_stamp(const KernelCtx& c, const float4* sorted, const uint32_t*
 void launch_band_list(const KernelCtx& c, const uint32_t* bits, const uint32_t* prefix, uint32_t nwords,
                       uint32_t* sv, uint32_t cap, const GroupMark& gm, Counters* ctr)
 {
-    k_band_list<<<persistent_blocks(c, nwords, 16), kThreads, 0, c.stream>>>(bits, prefix, nwords, sv, cap, gm, ctr);
+    k_band_list<<<persistent_blocks(c, nwords, 16), bs(c), 0, c.stream>>>(bits, prefix, nwords, sv, cap, gm, ctr);
     ++g_launches;
 }
 
@@ -1132,7 +1144,7 @@ void launch_smooth(const KernelCtx& c, const float4* sorted, uint32_t n, const u
     // warps may walk the union of their windows when the cull radius stays
     // below two cells (see k_smooth)
     const int coop_ok = (R * 1.0001f + 1e-4f * sp.cs) < 2.0f * sp.cs * 0.9999f ? 1 : 0;
-    k_smooth<<<blocks_for(n), kThreads, 0, c.stream>>>(sorted, n, ranges, sp, R, 1.0f / R, sqrt_threshold(R, false),
+    k_smooth<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(sorted, n, ranges, sp, R, 1.0f / R, sqrt_threshold(R, false),
                                                        coop_ok, oml, lambda, mass, mean, mean32,
                                                        smoothed);
     ++g_launches;
@@ -1152,7 +1164,7 @@ void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
 
 void launch_mc_classify(const KernelCtx& c, const McArgs& a, Counters* ctr)
 {
-    k_mc_classify<<<persistent_blocks(c, a.cap_band, 16), kThreads, 0, c.stream>>>(a, ctr);
+    k_mc_classify<<<persistent_blocks(c, a.cap_band, 16), bs(c), 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
 
@@ -1173,7 +1185,7 @@ void launch_mc_offsets(const KernelCtx& c, const McArgs& a, Counters* ctr, uint3
 
 void launch_mc_generate(const KernelCtx& c, const McArgs& a, Counters* ctr)
 {
-    k_mc_generate<<<persistent_blocks(c, a.cap_valid, 16), kThreads, 0, c.stream>>>(a, ctr);
+    k_mc_generate<<<persistent_blocks(c, a.cap_valid, 16), bs(c), 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
 
@@ -1181,7 +1193,7 @@ void launch_particle_flags(const KernelCtx& c, const uint32_t* skeys, const uint
                            uint32_t n, uint32_t* out)
 {
     if (!n) return;
-    k_particle_flags<<<blocks_for(n), kThreads, 0, c.stream>>>(skeys, surf, psurf, n, out);
+    k_particle_flags<<<blocks_for(n, bs(c)), bs(c), 0, c.stream>>>(skeys, surf, psurf, n, out);
     ++g_launches;
 }
 

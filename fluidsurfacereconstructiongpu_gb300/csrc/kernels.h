@@ -17,6 +17,7 @@ struct KernelCtx {
     cudaStream_t stream;
     int num_sms;
     int grid_div = 1;  // grid-stride kernels launch num_sms * per_sm / grid_div blocks (batches run frames side by side)
+    int block = 256;   // threads per block of the per-item and warp-staged kernels: 128 or 256 (batch autotuner)
 };
 
 // spatial hashing: keys[i] = cell id, vals[i] = i.

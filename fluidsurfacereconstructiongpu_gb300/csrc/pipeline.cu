@@ -287,7 +287,7 @@ fsr_status frame_enqueue(fsr_handle* h, const FramePlan& fp, const float* d_xyz,
     const bool yu13 = p.method == FSR_METHOD_YU13;
     const bool akinci = p.method == FSR_METHOD_AKINCI12;
     const bool keep = (p.flags & FSR_FLAG_KEEP_INTERMEDIATES) != 0;
-    const KernelCtx kc{st, h->num_sms, h->grid_div};
+    const KernelCtx kc{st, h->num_sms, h->grid_div, h->block};
     Counters* ctr = (Counters*)h->ctr.ptr;
     const float h_r = hdr.kernel_radius;
     const float h2 = h_r * h_r;

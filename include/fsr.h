@@ -314,6 +314,8 @@ typedef struct fsr_batch_tuning {
     float graph_ms;               /* one graph launch (the autotuner's best) */
     float frames_ms;              /* the same frames one after another, one
                                      synchronised fsr_reconstruct-style run each */
+    uint32_t block_threads;       /* threads per block of the per-item and
+                                     warp-staged kernels (128 or 256) */
 } fsr_batch_tuning;
 
 /* params: four fsr_params indexed by fsr_method (NULL: fsr_default_params

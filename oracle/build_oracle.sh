@@ -17,7 +17,17 @@ P1=$!
 P2=$!
 "${CXX:-g++}" -std=c++17 -O2 -fPIC -shared -o "$OUT/libio_port.so" "$HERE/io_port.cpp" &
 P3=$!
+# the launchers of the reference's own kernels (oracle/ref_gpu): they load
+# the cubin that oracle/ref_gpu/build_ref_gpu.sh builds from the reference's
+# sources where those are present, and is shipped with the other build
+# products elsewhere
+NVCC="${CUDA_HOME:-/usr/local/cuda}/bin/nvcc"
+"$NVCC" -gencode arch=compute_103a,code=sm_103a -std=c++17 -O2 -Xcompiler -fPIC -shared \
+  -I"$(dirname "$HERE")/include" -o "$OUT/libref_gpu.so" "$HERE/ref_gpu/ref_launchers.cu" \
+  -L"${CUDA_HOME:-/usr/local/cuda}/lib64/stubs" -lcuda &
+P4=$!
 wait "$P1"
 wait "$P2"
 wait "$P3"
-echo "build_oracle: wrote $OUT/liboracle32.so $OUT/liboracle64.so $OUT/libio_port.so"
+wait "$P4"
+echo "build_oracle: wrote $OUT/liboracle32.so $OUT/liboracle64.so $OUT/libio_port.so $OUT/libref_gpu.so"

@@ -129,6 +129,24 @@ static inline uint64_t cells_of(const o_gridinfo* g)
 }
 
 int o_real_bytes(void) { return (int)sizeof(real_t); }
+
+/* The marching-cubes tables in the reference's layout (MarchingCubesHelper.cpp:
+ * 3-577): edge flags per case, triangle edge lists of 16 ints per case (-1
+ * terminated), vertex counts per case, and the two corners of each edge.
+ * For uploading to the reference's own kernels (oracle/ref_gpu). */
+void o_mc_reference_tables(uint32_t edge_flags[256], int32_t tri[256 * 16], uint32_t nverts[256],
+                           uint32_t edge_corners[24])
+{
+    for (unsigned c = 0; c < 256; ++c) {
+        edge_flags[c] = fsr_o_edge_flags(c);
+        nverts[c] = fsr_o_num_vertices(c);
+        for (unsigned k = 0; k < 16; ++k) tri[16 * c + k] = k < 15 ? fsr_o_tri_edge(c, k) : -1;
+    }
+    for (unsigned e = 0; e < 12; ++e) {
+        edge_corners[2 * e] = (uint32_t)FSR_O_EDGE[e][0];
+        edge_corners[2 * e + 1] = (uint32_t)FSR_O_EDGE[e][1];
+    }
+}
 int o_is_reference(void) { return 0; }
 int o_set_threads(int n)
 {

@@ -1,12 +1,17 @@
-// Test helper: calls the reference-ABI launchers of libfsr_gb300.so from C++
+// Test helper: calls the reference-ABI launchers of a library from C++
 // with by-value structs, exactly as the reference's host classes do, behind
-// wrappers that take pointers (so the Python test never passes large
-// structs by value through ctypes).  Compiled by tests/test_gpu_compat.py.
+// wrappers that take pointers (so Python never passes large structs by
+// value through ctypes).  Compiled by oracle/ref_gpu/flow.py against
+// libfsr_gb300.so (the compatibility layer, csrc/compat.cu) or against
+// oracle/_build/libref_gpu.so (the reference's own kernels).
 #include "fsr_compat.h"
 
 extern "C" {
 
-void w_bindTextures() { bindTextures(nullptr, nullptr, nullptr, nullptr); }
+void w_bindTextures(uint* edge, int* tri, uint* nverts, uint* edge_corners)
+{
+    bindTextures(edge, tri, nverts, edge_corners);
+}
 
 void w_launchSpatialGridBuilding(const ParticleArray* p, const ScalarFieldGrid* d, uint n,
                                  const ParticleIndexRangeGrid* r, const DensityGrid* f, const GridInfo* gi)

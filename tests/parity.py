@@ -134,6 +134,18 @@ def compare_frame(rec, o32, o64, method: str, h: float) -> dict:
 
 
 def compare_frame_fullsize(rec, o32, o64, method: str, h: float, sample_seed: int = 0) -> dict:
+    """See _compare_frame_fullsize; prints what was measured before a failed
+    check is reported."""
+    rep = {}
+    try:
+        return _compare_frame_fullsize(rec, o32, o64, method, h, rep)
+    except AssertionError:
+        import json
+        print("PARTIAL_REPORT " + json.dumps({k: v for k, v in rep.items() if k != "field_worst"}), flush=True)
+        raise
+
+
+def _compare_frame_fullsize(rec, o32, o64, method: str, h: float, rep: dict) -> dict:
     """Parity of a large frame (the benchmark's sizes).
 
     Up to the band every integer equals the FP32 oracle's (the reference's
@@ -150,7 +162,6 @@ def compare_frame_fullsize(rec, o32, o64, method: str, h: float, sample_seed: in
     where the FP32 oracle's cases differ from the GPU's are counted and, for
     each, it is recorded which side agrees with FP64."""
     from oracle import pipeline as P
-    rep = {}
     assert np.array_equal(rec.debug("perm"), o32.perm), "stable sort order differs"
     assert np.array_equal(rec.debug("ranges"), o32.ranges), "cell ranges differ"
     assert np.array_equal(rec.debug("sorted_xyz"), o32.pos), "sorted positions differ"
@@ -167,6 +178,12 @@ def compare_frame_fullsize(rec, o32, o64, method: str, h: float, sample_seed: in
         rel = np.linalg.norm(G - o64.G, axis=1) / np.linalg.norm(o64.G, axis=1)
         rep["involved_particles"] = int(o32.inv.size)
         rep["G_rel_max"] = float(rel.max()) if rel.size else 0.0
+        if rel.size:
+            det = np.linalg.det(G.reshape(-1, 3, 3).astype(np.float64))
+            det64 = np.linalg.det(o64.G.reshape(-1, 3, 3))
+            rep["G_rel_median"] = float(np.median(rel))
+            rep["detG_rel_max"] = float(np.max(np.abs(det - det64) / np.abs(det64)))
+            rep["detG_rel_mean_signed"] = float(np.mean((det - det64) / np.abs(det64)))
         assert rep["G_rel_max"] <= 1e-5, f"G relative error {rep['G_rel_max']:.3e}"
     sv = rec.debug("band")
     assert np.array_equal(sv, o32.sv), "band vertices differ"

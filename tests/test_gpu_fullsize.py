@@ -1,7 +1,16 @@
-"""Checks on the 1M-particle anisotropic frame (the benchmark's workload) at full size.
+"""Checks on the anisotropic frames at full size: the 1M-particle frame of the
+benchmark and the 8M-particle frame (a 200^3 lattice at r = 0.002, 1020^3
+scalar grid).
 
-The oracle needs the dense scalar grid and takes minutes at this size, so the
-full-size frame is checked through properties that hold at any size:
+The dense oracle does not fit the 8M frame (its scalar grid alone holds
+1.06e9 vertices), so these frames are checked through properties that hold
+at any size, on samples evaluated in FP64 from the definitions:
+
+* smoothed positions and G of 2,000 sampled particles against an FP64
+  evaluation of calculationOfMeanAndSmoothParticles (ReconstructionCUDA.cu:
+  598-658) and calculationOfTransformMatricesForParticles (cu:689-827) over
+  the particles within R (a k-d tree instead of the cell walk: the same
+  neighbours), within 1e-6 absolute and 1e-5 relative;
 
 * the field at 1,000 sampled band vertices equals an FP64 evaluation of the
   anisotropic kernel sum (computationOfScalarFieldGrid, ReconstructionCUDA.cu:
@@ -23,18 +32,24 @@ SETTINGS = dict(smoothing_lambda=0.9, aniso_radius_over_h=1.0, cell_size_scale=1
 SIGMA = np.float32(315.0) / (np.float32(64.0) * np.float32(3.1415926535898))
 
 
-@pytest.fixture(scope="module")
-def frame():
+FRAMES = {
+    "aniso1m": lambda s: s.dam_break(1 << 20, r=0.004, seed=2),
+    "aniso8m": lambda s: s.lattice_cube(200, 0.002, seed=1),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(FRAMES))
+def frame(request):
     import torch
     from fluidsurfacereconstructiongpu_gb300 import api, synthetic
-    fr = synthetic.dam_break(1 << 20, r=0.004, seed=2)
+    fr = FRAMES[request.param](synthetic)
     rec = api.Reconstructor("yu13", 0, keep_intermediates=True, **SETTINGS)
     x = torch.from_numpy(fr.pos).cuda()
     d = torch.from_numpy(fr.density).cuda()
     rec.reconstruct(x, d, api.header_of(fr))
     out = dict(fr=fr, stats=rec.stats(), mesh=rec.mesh(), band=rec.debug("band"), field=rec.debug("field"),
                sorted=rec.debug("sorted_xyz"), ranges=rec.debug("ranges"), inv=rec.debug("involved_counts"),
-               smoothed=rec.debug("smoothed"), G=rec.debug("G"))
+               smoothed=rec.debug("smoothed"), G=rec.debug("G"), perm=rec.debug("perm"))
     rec.reconstruct(x, d, api.header_of(fr))
     out["mesh2"] = rec.mesh()
     rec.close()
@@ -124,3 +139,47 @@ def test_mesh_vertices_on_grid_edges(frame):
     ln = np.linalg.norm(nrm.astype(np.float64), axis=1)
     unit = np.abs(ln - 1.0) < 1e-5
     assert unit.mean() >= 0.999, unit.mean()
+
+
+def test_smoothing_and_G_match_fp64_definition(frame):
+    """FP64 means, smoothed positions and G of sampled particles from their
+    definitions, against the GPU's (sorted order)."""
+    from scipy.spatial import cKDTree
+    fr = frame["fr"]
+    pos = frame["sorted"].astype(np.float64)
+    h = float(np.float32(fr.h))
+    R = float(np.float32(np.float32(fr.h) * np.float32(SETTINGS["aniso_radius_over_h"])))
+    lam = SETTINGS["smoothing_lambda"]
+    tree = cKDTree(pos)
+    ranges, inv = frame["ranges"], frame["inv"]
+    counts = np.where(ranges[:, 0] == 0xFFFFFFFF, 0, ranges[:, 1].astype(np.int64) - ranges[:, 0])
+    involved = np.repeat(inv > 0, counts)
+    rng = np.random.default_rng(11)
+    rows = rng.choice(pos.shape[0], 2000, replace=False)
+    worst_sm = worst_g = 0.0
+    n_g = 0
+    for i in rows:
+        j = np.array(tree.query_ball_point(pos[i], R * (1 + 1e-6)), np.int64)
+        d = np.sqrt(np.sum((pos[j] - pos[i]) ** 2, axis=1))
+        w = np.where(d < R, 1.0 - (d / R) ** 3, 0.0)
+        mean = (w[:, None] * pos[j]).sum(axis=0) / w.sum()
+        sm = (1.0 - lam) * pos[i] + lam * mean
+        worst_sm = max(worst_sm, float(np.abs(frame["smoothed"][i] - sm).max()))
+        if not involved[i]:
+            continue
+        k = np.array(tree.query_ball_point(mean, R * (1 + 1e-6)), np.int64)
+        v = pos[k] - mean
+        dk = np.sqrt(np.sum(v * v, axis=1))
+        if np.sum(dk <= R) < 25 or np.min(np.abs(dk - R)) < 1e-6 * R:
+            continue  # isolated (G = I/h), or a neighbour on the count boundary
+        wk = np.where(dk < R, 1.0 - (dk / R) ** 3, 0.0)
+        C = (h * h * np.eye(3) + np.einsum("n,ni,nj->ij", wk, v, v)) / wk.sum()
+        ev, V = np.linalg.eigh(C)
+        s = np.maximum(np.abs(ev), np.abs(ev).max() / 4.0)
+        G = (V / s) @ V.T * (np.cbrt(np.prod(s)) / h)
+        g = frame["G"][i].reshape(3, 3).astype(np.float64)
+        worst_g = max(worst_g, float(np.linalg.norm(g - G) / np.linalg.norm(G)))
+        n_g += 1
+    assert n_g > 500
+    assert worst_sm <= 1e-6, worst_sm
+    assert worst_g <= 1e-5, worst_g
