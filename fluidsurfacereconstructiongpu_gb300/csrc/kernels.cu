@@ -472,7 +472,10 @@ __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src,
 //   neighbours; the covariance is taken about this mean, and the smoothed
 //   positions are formed from it.  mean.w = its weight sum (the adjoint
 //   divides by it); smoothed.w = m / rho.
-__global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ sorted, uint32_t n,
+#ifndef FSR_SMOOTH_MIN_BLOCKS
+#define FSR_SMOOTH_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
                                                      float R_rcp, float R_lt2, int coop_ok, float one_minus_lambda,
                                                      float lambda, float mass, float4* __restrict__ mean,
@@ -565,11 +568,11 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const float4* __restrict__ 
             for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
-                for (uint32_t i = beg; i < end; ++i) {
-                    add(__ldg(&sorted[i]));
-                    if (((i - beg) & 31u) == 31u) fold();  // chunks of 32, as in the staged walk
+                for (uint32_t base = beg; base < end; base += 32) {  // chunks of 32, as in the staged walk
+                    const uint32_t lim = min(end, base + 32u);
+                    for (uint32_t i = base; i < lim; ++i) add(__ldg(&sorted[i]));
+                    fold();
                 }
-                fold();
             }
     }
     if (!active) return;
@@ -620,6 +623,10 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
     {
         const float4 m32 = act ? a.mean32[t] : p;
         dm = sqrtf(fmaf(m.x - m32.x, m.x - m32.x, fmaf(m.y - m32.y, m.y - m32.y, (m.z - m32.z) * (m.z - m32.z))));
+#ifdef FSR_COV_UNIFORM_DM
+        // the warp's largest offset: thresholds uniform across the warp
+        dm = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dm)));
+#endif
     }
     const float cr = cull_radius(a.R, a.sp.cs) + 2.0f * dm;
     // a candidate within R of either mean lies within R + dm of m

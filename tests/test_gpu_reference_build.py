@@ -53,6 +53,10 @@ def test_reference_kernels_match_oracle(method, name):
     if method == "yu13":
         assert np.array_equal(got["ninv"], o.ninv), "involved counts"
         rep["mean_abs_max_vs_fp32"] = float(np.abs(got["mean"] - o.mean32).max())
+        # G of the reference's SVD (SVD3.cuh) against the FP64 eigen-decomposition
+        rel = np.linalg.norm(got["G"] - o64.G, axis=1) / np.linalg.norm(o64.G, axis=1)
+        rep["G_rel_max_vs_fp64"] = float(rel.max())
+        rep["G_rel_median_vs_fp64"] = float(np.median(rel))
     band_diff = int(np.sum(got["is_surf"] != o.is_surf))
     rep["band_vertices"] = int(o.sv.size)
     rep["band_diffs"] = band_diff

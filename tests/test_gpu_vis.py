@@ -5,7 +5,11 @@ The expected file is written here the way saveMiddleDataToVisFile writes it
 (ReconstructorGPUOursZB05.cpp:104-230, ReconstructorGPUOursYu13.cpp:285-420,
 ReconstructorGPUAkinci12.cpp:290-420: std::ostream, %g floats, lists as
 "count" then "i " per entry), from the FP32 oracle's arrays; the GPU's file
-must match it byte for byte.
+must match it byte for byte.  The one exception is the anisotropic path's
+smoothed positions: the library forms them from a compensated mean (they
+are within 1e-7 of FP64, the reference's FP32 ones are not), so that block
+is written from the frame's own smoothed positions, which are checked
+against the FP64 oracle within the parity bar (1e-6).
 """
 import numpy as np
 import pytest
@@ -17,7 +21,7 @@ def _g(x) -> str:
     return "%g" % float(np.float32(x))
 
 
-def _expected(o, fr, mesh_name):
+def _expected(o, fr, mesh_name, smoothed=None):
     sp, sc = o.spatial, o.scalar
     out = []
     for g in (sp, sc):
@@ -37,7 +41,7 @@ def _expected(o, fr, mesh_name):
     out.append(lst(np.flatnonzero(o.flag > 0), o.flag.size > 0))
     if o.method == "yu13":
         out.append("%d\n" % n)
-        out += ["%s %s %s\n" % (_g(p[0]), _g(p[1]), _g(p[2])) for p in o.smoothed]
+        out += ["%s %s %s\n" % (_g(p[0]), _g(p[1]), _g(p[2])) for p in (o.smoothed if smoothed is None else smoothed)]
     else:
         out.append("0\n")
     out.append(lst(o.sv))
@@ -60,10 +64,11 @@ def test_vis_matches_reference_layout(tmp_path, method):
     from fluidsurfacereconstructiongpu_gb300 import api, synthetic
     from oracle import pipeline as P
     fr = synthetic.lattice_cube(12, 0.0125, seed=3, origin=(0.3, 0.3, 0.3))
-    rec = api.Reconstructor(method, 0)
+    rec = api.Reconstructor(method, 0, keep_intermediates=True)
     rec.reconstruct(torch.from_numpy(fr.pos).cuda(), torch.from_numpy(fr.density).cuda(), api.header_of(fr))
     path = tmp_path / "frame_000.vis"
     rec.write_vis(str(path), "frame_000.obj")
+    smoothed = rec.debug("smoothed") if method == "yu13" else None
     rec.close()
     p = api.default_params(method)
     params = P.FrameParams(method="akinci" if method == "akinci12" else method, h=fr.h,
@@ -71,7 +76,10 @@ def test_vis_matches_reference_layout(tmp_path, method):
                            lam=p.smoothing_lambda, aniso_radius=p.aniso_radius_over_h * fr.h,
                            min_neighbors=p.min_neighbors)
     o = P.run_frame("oracle32", fr.pos, fr.density, fr.bbox_min, fr.bbox_max, params)
-    want = _expected(o, fr, "frame_000.obj")
+    if smoothed is not None:
+        o64 = P.run_frame("oracle64", fr.pos, fr.density, fr.bbox_min, fr.bbox_max, params)
+        assert np.abs(smoothed - o64.smoothed).max() <= 1e-6
+    want = _expected(o, fr, "frame_000.obj", smoothed)
     got = path.read_bytes()
     if got != want:
         a, b = got.split(b"\n"), want.split(b"\n")
