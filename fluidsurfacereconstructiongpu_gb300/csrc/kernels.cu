@@ -463,7 +463,7 @@ __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src,
 //   it must be the reference's bit for bit.
 // * mean: the same quantity to near FP64 accuracy, as x_i + sum(w (x_j -
 //   x_i)) / sum(w).  The offsets x_j - x_i are exact (Sterbenz) and at most R
-//   long, so their sums stay small; they are summed per chunk of 32
+//   long, so their sums stay small; they are summed per chunk of 32 to 63
 //   candidates and the chunk sums, like the weights, are added with Kahan
 //   compensation (neighbouring particles sum nearly the same candidates in
 //   the same order, so the rounding errors of long plain sums would be
@@ -473,7 +473,7 @@ __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src,
 //   positions are formed from it.  mean.w = its weight sum (the adjoint
 //   divides by it); smoothed.w = m / rho.
 #ifndef FSR_SMOOTH_MIN_BLOCKS
-#define FSR_SMOOTH_MIN_BLOCKS 1
+#define FSR_SMOOTH_MIN_BLOCKS 4  // 64 registers: 4 blocks of 256 threads per SM (measured best of 1, 4, 5, 6)
 #endif
 __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(const float4* __restrict__ sorted, uint32_t n,
                                                      const uint2* __restrict__ ranges, Grid sp, float R,
@@ -512,12 +512,16 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
         cy = __fmaf_rn(-wt, dy, cy);
         cz = __fmaf_rn(-wt, dz, cz);
     };
+    // the chunk sums join the totals once at least 32 candidates (staged or
+    // walked) have been added since the last time
+    uint32_t since = 0;
     auto fold = [&]() {
         tw.add(cw);
         tx.add(cx);
         ty.add(cy);
         tz.add(cz);
         cw = cx = cy = cz = 0.f;
+        since = 0;
     };
     auto row_range = [&](int x0, int x1, int yy, int zz, uint32_t& beg, uint32_t& end) {
         const uint32_t c0 = lin3(x0, yy, zz, sp);
@@ -558,7 +562,8 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
                     const uint32_t cnt = stage_in_box(sorted, base, end, box, sq, lane);
                     __syncwarp();
                     for (uint32_t k = 0; k < cnt; ++k) add(sq[k]);
-                    fold();
+                    since += cnt;
+                    if (since >= 32) fold();
                     __syncwarp();
                 }
             }
@@ -568,14 +573,16 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
             for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
                 uint32_t beg, end;
                 row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
-                for (uint32_t base = beg; base < end; base += 32) {  // chunks of 32, as in the staged walk
+                for (uint32_t base = beg; base < end; base += 32) {
                     const uint32_t lim = min(end, base + 32u);
                     for (uint32_t i = base; i < lim; ++i) add(__ldg(&sorted[i]));
-                    fold();
+                    since += lim - base;
+                    if (since >= 32) fold();
                 }
             }
     }
     if (!active) return;
+    fold();
     // ws >= 1: the particle itself has weight 1
     mx = __fdiv_rn(mx, ws);
     my = __fdiv_rn(my, ws);
@@ -623,10 +630,6 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
     {
         const float4 m32 = act ? a.mean32[t] : p;
         dm = sqrtf(fmaf(m.x - m32.x, m.x - m32.x, fmaf(m.y - m32.y, m.y - m32.y, (m.z - m32.z) * (m.z - m32.z))));
-#ifdef FSR_COV_UNIFORM_DM
-        // the warp's largest offset: thresholds uniform across the warp
-        dm = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(dm)));
-#endif
     }
     const float cr = cull_radius(a.R, a.sp.cs) + 2.0f * dm;
     // a candidate within R of either mean lies within R + dm of m

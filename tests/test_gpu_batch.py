@@ -109,3 +109,24 @@ def test_batch_rejects_bad_frames():
         b.reconstruct([("zb05", bad, fr.density, api.header_of(fr))], autotune=False)
     assert e.value.status == 2
     b.close()
+
+
+def test_batch_at_the_benchmark_sizes():
+    """The first 12 frames of the benchmark's batch (20k-400k particles,
+    mixed fields, the anisotropic frames with the 1M frame's settings):
+    every frame equals the single-frame path bit for bit, with the batch's
+    autotuned lanes, grid division and block shape."""
+    import torch
+    import bench
+    from fluidsurfacereconstructiongpu_gb300 import api
+    frames = bench.batch_frames()[:12]
+    params = bench.BATCH["params"]
+    b = api.Batch(0, params=params)
+    args = [(m, torch.from_numpy(fr.pos).cuda(), torch.from_numpy(fr.density).cuda(), api.header_of(fr))
+            for m, fr in frames]
+    b.reconstruct(args)
+    t = b.tuning()
+    assert t.block_threads in (128, 256)
+    for i, (m, fr) in enumerate(frames):
+        _check_same(b, i, m, fr, **params[m])
+    b.close()
