@@ -120,6 +120,40 @@ struct CovAccum {
     }
 };
 
+// The same sums with the compensation per chunk instead of per term: each
+// term enters a plain FP32 chunk sum (one FMA per entry), and after every
+// 32 or more candidates the chunk sums join Kahan-compensated totals.  The
+// chunks are short, so their own rounding stays at a few ulps of a chunk,
+// and the totals keep the compensation of the per-term form at an eighth of
+// its instructions.
+struct CovChunkAccum {
+    CovAccum tot;
+    float w = 0.f, c11 = 0.f, c22 = 0.f, c33 = 0.f, c12 = 0.f, c13 = 0.f, c23 = 0.f;
+    __device__ __forceinline__ void add(float vx, float vy, float vz, float s)
+    {
+        const float wt = 1.0f - s * s * s;
+        w += wt;
+        const float wx = wt * vx, wy = wt * vy;
+        c11 = fmaf(wx, vx, c11);
+        c22 = fmaf(wy, vy, c22);
+        c33 = fmaf(wt * vz, vz, c33);
+        c12 = fmaf(wx, vy, c12);
+        c13 = fmaf(wx, vz, c13);
+        c23 = fmaf(wy, vz, c23);
+    }
+    __device__ __forceinline__ void fold()
+    {
+        tot.wsum.add(w);
+        tot.c11.add(c11);
+        tot.c22.add(c22);
+        tot.c33.add(c33);
+        tot.c12.add(c12);
+        tot.c13.add(c13);
+        tot.c23.add(c23);
+        w = c11 = c22 = c33 = c12 = c13 = c23 = 0.f;
+    }
+};
+
 // G for a particle with nn neighbours within R: I / h for isolated particles
 // (fewer than min_neighbors), else (1/h) cbrt(s1 s2 s3) V diag(1/s) V^T with
 // the eigenvalues s clamped from below at max(s)/4.  Returns the largest

@@ -599,9 +599,10 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
 
 // calculationOfTransformMatricesForParticles (cu:689-827) for every
 // particle of an involved cell.  The neighbour count (dist <= r about the
-// FP32 mean, cu:746) is exact; the covariance is accumulated with Kahan
-// compensation; the eigen-decomposition runs in FP32 and is redone in FP64
-// when the covariance's condition number exceeds 1e4.
+// FP32 mean, cu:746) is exact; the covariance is accumulated in chunk sums
+// joined with Kahan compensation (CovChunkAccum); the eigen-decomposition
+// runs in FP32 and is redone in FP64 when the covariance's condition number
+// exceeds 1e4.
 // Output record per particle: (x,y,z smoothed, r2max) (G row 0, coef)
 // (G row 1, 0) (G row 2, 0) with coef = sigma det(G) m / rho.
 // Blocks of two warps: a warp without involved particles exits at once, and
@@ -645,7 +646,12 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
     const Window w = narrow(window(cell1(p.x, a.sp.min[0], a.sp.cs), cell1(p.y, a.sp.min[1], a.sp.cs),
                                    cell1(p.z, a.sp.min[2], a.sp.cs), 2, a.sp),
                             m.x, m.y, m.z, cr, a.sp);
-    CovAccum acc;
+    CovChunkAccum acc;
+    uint32_t since = 0;  // candidates taken since the chunk sums last joined the totals
+    auto fold = [&]() {
+        acc.fold();
+        since = 0;
+    };
     uint32_t nn = 0;
     // d > R: neither counted nor weighed
     auto take = [&](const float4& q) {
@@ -707,6 +713,8 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
                         if (n3) take(q3);
                     }
                     for (; k < cnt; ++k) take(sq[k]);
+                    since += cnt;
+                    if (since >= 32) fold();
                     __syncwarp();
                 }
             }
@@ -727,17 +735,21 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
                     if (n1) take(q1);
                     if (n2) take(q2);
                     if (n3) take(q3);
+                    since += 4;
+                    if (since >= 32) fold();
                 }
                 for (; i < end; ++i) take(__ldg(&a.sorted[i]));
             }
     }
+    fold();
+    const CovAccum& sums = acc.tot;
     float G[9];
-    const float rmax = covariance_to_G(acc, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
+    const float rmax = covariance_to_G(sums, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
     if (a.crec) {  // the normalised covariance for the adjoint (the same expressions as covariance_to_G)
         const bool used = nn >= a.min_neighbors;
-        const float iw = used ? 1.0f / acc.wsum.s : 0.f;
-        a.crec[2ull * t] = make_float4((a.h2 + acc.c11.s) * iw, acc.c12.s * iw, acc.c13.s * iw, (a.h2 + acc.c22.s) * iw);
-        a.crec[2ull * t + 1] = make_float4(acc.c23.s * iw, (a.h2 + acc.c33.s) * iw, acc.wsum.s, used ? 1.f : 0.f);
+        const float iw = used ? 1.0f / sums.wsum.s : 0.f;
+        a.crec[2ull * t] = make_float4((a.h2 + sums.c11.s) * iw, sums.c12.s * iw, sums.c13.s * iw, (a.h2 + sums.c22.s) * iw);
+        a.crec[2ull * t + 1] = make_float4(sums.c23.s * iw, (a.h2 + sums.c33.s) * iw, sums.wsum.s, used ? 1.f : 0.f);
     }
     const float det = G[0] * G[4] * G[8] + G[1] * G[5] * G[6] + G[2] * G[3] * G[7] - G[0] * G[5] * G[7] -
                       G[1] * G[3] * G[8] - G[2] * G[4] * G[6];
