@@ -76,7 +76,9 @@ __global__ void k_mc_backward(BwdArgs a, const Counters* ctr)
     }
 }
 
-// keys (window centres) holding a band vertex with a non-zero field gradient
+// keys (window centres) holding a band vertex with a non-zero field gradient;
+// the first vertex to mark a key appends it to the list the grouped
+// adjoints take their groups from
 __global__ void k_mark_keys(BwdArgs a, const Counters* ctr)
 {
     const uint32_t nb = min(ctr->n_band, a.cap_band);
@@ -88,7 +90,8 @@ __global__ void k_mark_keys(BwdArgs a, const Counters* ctr)
         const int cx = cell1(vpos1(x, a.sc.min[0], a.sc.cs), a.sp.min[0], a.sp.cs);
         const int cy = cell1(vpos1(y, a.sc.min[1], a.sc.cs), a.sp.min[1], a.sp.cs);
         const int cz = cell1(vpos1(z, a.sc.min[2], a.sc.cs), a.sp.min[2], a.sp.cs);
-        a.gkey[((uint32_t)cz * ky + cy) * kx + cx] = 1;
+        const uint32_t key = ((uint32_t)cz * ky + cy) * kx + cx;
+        if (a.gkey[key] == 0u && atomicExch(&a.gkey[key], 1u) == 0u) a.glist[4 + atomicAdd(&a.glist[0], 1u)] = key;
     }
 }
 
@@ -660,7 +663,7 @@ void launch_backward(const KernelCtx& c, const BwdArgs& a, const CovArgs* cov, c
         fb.invol = a.invol;
         fb.cell_rmax = a.cell_rmax;
         fb.gphi = a.gphi;
-        fb.gkey = a.gkey;
+        fb.glist = a.glist;
         fb.gsmooth = a.gsmooth;
         fb.gG = a.gG;
         fb.sigma = a.sigma;

@@ -17,7 +17,9 @@ struct BwdArgs {
     const uint64_t* tri;     // packed marching-cubes triangle table (device)
     const float* gmesh;      // dL/d mesh vertex positions, 3 floats each
     float* gphi;             // dL/dphi per band vertex (zeroed)
-    uint8_t* gkey;           // per window-centre key: holds a vertex with dL/dphi != 0 (zeroed)
+    uint32_t* gkey;          // per window-centre key: holds a vertex with dL/dphi != 0 (zeroed)
+    uint32_t* glist;         // [0] keys listed, [1] [2] work counters of the grouped adjoints (zeroed),
+                             // [4 ..] the keys with gkey set, in the order k_mark_keys met them
     const float4* sorted;
     const uint32_t* skeys;
     const uint32_t* perm;

@@ -64,7 +64,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     const uint64_t keys = (uint64_t)(sp.res[0] + 1) * (sp.res[1] + 1) * (sp.res[2] + 1);
     const uint64_t nn = std::max<uint64_t>(n, 1);
     BCK(h->gphi.ensure(4ull * h->cap_band));
-    BCK(h->gkey.ensure(keys));
+    BCK(h->gkey.ensure(4ull * keys));
+    BCK(h->gklist.ensure(4ull * (keys + 4)));
     BCK(h->gx.ensure(16ull * nn));
     BCK(h->gscalar.ensure(16));
     if (p.method == FSR_METHOD_YU13) {
@@ -77,7 +78,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
         BCK(cudaMemcpy(h->tri.ptr, mc::kTriPacked, sizeof(mc::kTriPacked), cudaMemcpyHostToDevice));
     }
     BCK(cudaMemsetAsync(h->gphi.ptr, 0, 4ull * h->cap_band, st));
-    BCK(cudaMemsetAsync(h->gkey.ptr, 0, keys, st));
+    BCK(cudaMemsetAsync(h->gkey.ptr, 0, 4ull * keys, st));
+    BCK(cudaMemsetAsync(h->gklist.ptr, 0, 16, st));
     BCK(cudaMemsetAsync(h->gx.ptr, 0, 16ull * nn, st));
     BCK(cudaMemsetAsync(h->gscalar.ptr, 0, 16, st));
     if (p.method == FSR_METHOD_YU13) {
@@ -98,7 +100,8 @@ extern "C" fsr_status fsr_backward(fsr_handle* h, const float* d_grad_mesh_pos, 
     a.tri = (const uint64_t*)h->tri.ptr;
     a.gmesh = d_grad_mesh_pos;
     a.gphi = (float*)h->gphi.ptr;
-    a.gkey = (uint8_t*)h->gkey.ptr;
+    a.gkey = (uint32_t*)h->gkey.ptr;
+    a.glist = (uint32_t*)h->gklist.ptr;
     a.sorted = (const float4*)h->sorted.ptr;
     a.skeys = h->skeys_ptr;
     a.perm = h->perm_ptr;

@@ -970,7 +970,7 @@ struct BwdGroupArgs {
     const uint8_t* invol;
     const float* reach;
     const float* gphi;
-    const uint8_t* gkey;
+    uint32_t* glist;
     float4* gsmooth;
     float4* gG;
     float sigma;
@@ -995,23 +995,34 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
     uint32_t* cstart = reinterpret_cast<uint32_t*>(cbox + 2 * nch_cap);
     uint32_t* cpre = cstart + 128;
     uint32_t* cinv = cpre + 129;
-    __shared__ uint32_t s_nv, s_tot, s_wsum[4];
+    __shared__ uint32_t s_nv, s_tot, s_wsum[4], s_next;
     __shared__ float4 s_lo, s_hi;
     const CandTables tabs{cstart, cpre, cinv};
 
+    __shared__ uint32_t s_g;
     const uint32_t nb = min(ctr->n_band, a.cap);
     const int tid = threadIdx.x, lane = tid & 31;
-    const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
+    const uint32_t nlist = a.glist[0];
 
-    for (uint32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
-        if (!a.gkey[g]) continue;  // uniform across the block
+    // the groups holding gradient vertices, handed out one per block from
+    // the list k_mark_keys built
+    for (;;) {
+        if (tid == 0) s_g = atomicAdd(&a.glist[1], 1u);
+        __syncthreads();
+        const uint32_t k = s_g;
+        __syncthreads();
+        if (k >= nlist) break;
+        const uint32_t g = a.glist[4 + k];
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
         const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
         const int nbox = nx * ny * nz;
 
         // 1. the group's vertices with dL/dphi != 0
-        if (tid == 0) s_nv = 0;
+        if (tid == 0) {
+            s_nv = 0;
+            s_next = 0;
+        }
         __syncthreads();
         for (int base = 0; base < nbox; base += kBT) {
             const int i = base + tid;
@@ -1072,9 +1083,15 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
         const float b0[3] = {glo.x, glo.y, glo.z}, b1[3] = {ghi.x, ghi.y, ghi.z};
         const uint32_t total = group_candidates(a.sp, a.ranges, a.invol, a.reach, c, b0, b1, tabs, s_wsum, &s_tot);
 
-        // 3. one candidate per thread, gradient kept in registers
-        for (uint32_t cb = 0; cb < total; cb += kBT) {
-            const uint32_t j = cb + tid;
+        // 3. one candidate per thread, gradient kept in registers; warps take
+        // the next 32 candidates as they finish, so that the group's slow
+        // candidates do not hold the others at the block's barrier
+        for (;;) {
+            uint32_t cb = 0;
+            if (lane == 0) cb = atomicAdd(&s_next, 32u);
+            cb = __shfl_sync(0xffffffffu, cb, 0);
+            if (cb >= total) break;
+            const uint32_t j = cb + lane;
             if (j >= total) continue;
             int cell;
             const uint32_t i = candidate(j, tabs, &cell);
@@ -1170,20 +1187,32 @@ __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, u
     float4* av = reinterpret_cast<float4*>(smem);  // active vertices: (v, dL/dphi)
     float4* am = av + vlist_cap;                    // ZB05: (mean - v, weight sum)
     float4* cbox = am + (TC01 ? 0 : vlist_cap);     // per 32 of them: lo, hi
-    __shared__ uint32_t s_nv, s_rb[9], s_re[9], s_rp[10];
+    __shared__ uint32_t s_nv, s_rb[9], s_re[9], s_rp[10], s_next;
     const uint32_t nb = min(ctr->n_band, a.cap_band);
     const int tid = threadIdx.x, lane = tid & 31;
     const uint32_t ngroups = (a.sp.res[0] + 1) * (a.sp.res[1] + 1) * (a.sp.res[2] + 1);
     const float h2 = a.h * a.h, inv_h2 = 1.0f / h2;
     const float cr = cull_radius(a.h, a.sp.cs), cr2 = cr * cr;
+    __shared__ uint32_t s_g;
+    const uint32_t nlist = a.glist[0];
 
-    for (uint32_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
-        if (!a.gkey[g]) continue;  // uniform across the block
+    // the groups holding gradient vertices, handed out one per block from
+    // the list k_mark_keys built
+    for (;;) {
+        if (tid == 0) s_g = atomicAdd(&a.glist[2], 1u);
+        __syncthreads();
+        const uint32_t k = s_g;
+        __syncthreads();
+        if (k >= nlist) break;
+        const uint32_t g = a.glist[4 + k];
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, a.ratio, c, lo, hi)) continue;
         const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
         const int nbox = nx * ny * nz;
-        if (tid == 0) s_nv = 0;
+        if (tid == 0) {
+            s_nv = 0;
+            s_next = 0;
+        }
         __syncthreads();
         for (int base = 0; base < nbox; base += kBT) {
             const int i = base + tid;
@@ -1258,7 +1287,14 @@ __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, u
         }
         __syncthreads();
         const uint32_t total = nv ? s_rp[9] : 0u;
-        for (uint32_t jj = tid; jj < total; jj += kBT) {
+        // one candidate per thread; warps take the next 32 as they finish
+        for (;;) {
+            uint32_t cb = 0;
+            if (lane == 0) cb = atomicAdd(&s_next, 32u);
+            cb = __shfl_sync(0xffffffffu, cb, 0);
+            if (cb >= total) break;
+            const uint32_t jj = cb + lane;
+            if (jj >= total) continue;
             int r = 0;
             while (r < 8 && s_rp[r + 1] <= jj) ++r;
             const uint32_t j = s_rb[r] + (jj - s_rp[r]);
@@ -1330,7 +1366,7 @@ bool launch_field_aniso_backward_grouped(const KernelCtx& c, const AnisoBwdArgs&
     a.invol = f.invol;
     a.reach = f.cell_rmax;
     a.gphi = f.gphi;
-    a.gkey = f.gkey;
+    a.glist = f.glist;
     a.gsmooth = f.gsmooth;
     a.gG = f.gG;
     a.sigma = f.sigma;

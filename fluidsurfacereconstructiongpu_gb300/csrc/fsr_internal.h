@@ -81,7 +81,7 @@ struct fsr_handle {
     fsr::DevBuf ctr;
     // backward pass
     fsr::DevBuf mv;                      // ZB05/Akinci12: per band vertex (mean - v, weight sum)
-    fsr::DevBuf gphi, gkey, gsmooth, gG, gmean, gx, gscalar, tri;
+    fsr::DevBuf gphi, gkey, gklist, gsmooth, gG, gmean, gx, gscalar, tri;  // gklist: keys with gradient vertices
 
     uint32_t cap_band = 0, cap_valid = 0, cap_mesh = 0;
     int grid_div = 1;                    // grid-stride kernels use num_sms * per_sm / grid_div blocks

@@ -142,7 +142,7 @@ struct AnisoBwdArgs {
     const uint8_t* invol;
     const float* cell_rmax;
     const float* gphi;
-    const uint8_t* gkey;
+    uint32_t* glist;  // the keys holding gradient vertices and the work counter (BwdArgs::glist)
     float4* gsmooth;
     float4* gG;
     float sigma;
