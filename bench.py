@@ -675,6 +675,23 @@ def main():
             frx = make_frame(wx)
             extra[name] = frame_leg(wx, frx, dev, stream, min(args.steps, 10), args.warmup, flush, fp32, peak)
             del frx
+        # the small plain workload (32^3 lattice, ZB05) at the reference's iso (-1e-4) and at 0.5
+        extra["plain32k"] = {}
+        for iso in (-1e-4, 0.5):
+            wx = dict(WORKLOADS["plain32k"], iso=iso)
+            frx = make_frame(wx)
+            r32 = api.Reconstructor("zb05", local, **recon_kwargs(wx))
+            h32 = api.header_of(frx)
+            x32 = torch.from_numpy(frx.pos).to(dev)
+            d32 = torch.from_numpy(frx.density).to(dev)
+            for _ in range(args.warmup):
+                r32.reconstruct(x32, d32, h32, stream)
+            ms32 = time_steps(lambda: r32.reconstruct(x32, d32, h32, stream), stream, min(args.steps, 10), flush)
+            s32 = r32.stats()
+            extra["plain32k"]["iso %g" % iso] = {
+                "particles": frx.n, "ms_per_step": float(np.mean(ms32)), "value": frx.n / (float(np.mean(ms32)) / 1e3),
+                "band_vertices": int(s32.n_band_vertices), "triangles": int(s32.n_mesh_vertices) // 3}
+            r32.close()
     batched = None
     if not args.no_batch:
         batched = run_batch_leg(dev, stream, min(args.steps, 10), args.warmup, flush)
@@ -745,6 +762,7 @@ def main():
             "fp32_peak_tflops": {"value": fp32, "source": "measured (fsr_measure_fp32_rate, FMA chains)"},
             "plain_path": extra.get("plain1m"),
             "aniso8m": extra.get("aniso8m"),
+            "plain32k": extra.get("plain32k"),
             "batched": batched,
             "gpu_launches": n_launch * args.steps,
             "roofline": roofline, "clocks": clocks, "cpu_baseline": cpu, "reference_gpu": ref_gpu}

@@ -170,6 +170,9 @@ __device__ __forceinline__ void load_record(const float4* __restrict__ grec, con
 
 // ---------------------------------------------------------------- forward
 constexpr int kFT = 128;                 // threads per block of the forward kernel
+#ifndef FSR_FIELD_MIN_BLOCKS
+#define FSR_FIELD_MIN_BLOCKS 6               // blocks per SM of the anisotropic field (80 registers)
+#endif
 constexpr int kFWarps = kFT / 32;
 constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept in registers)
 constexpr int kPassVerts = 32 * kPassTiles;
@@ -567,7 +570,7 @@ __device__ __forceinline__ float unscaled_sum(const float* m, float zx, float zy
 // tile the warp keeps the candidates whose support sphere reaches the
 // tile's box and each lane adds their terms for its vertex of that tile.
 // A vertex's sum takes the candidates in window order.
-__global__ void __launch_bounds__(kFT, 6) k_field_aniso_grouped(GroupArgs a, uint32_t ratio, Counters* ctr)
+__global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_grouped(GroupArgs a, uint32_t ratio, Counters* ctr)
 {
     __shared__ WarpSlice slices[kFWarps];
     const int lane = threadIdx.x & 31;

@@ -118,3 +118,15 @@ def test_host_path_matches_device_path():
     m2 = rec.mesh()
     assert np.array_equal(m1.positions, m2.positions) and np.array_equal(m1.normals, m2.normals)
     rec.close()
+
+
+def test_zb05_plain_small_workload_baseline_iso():
+    """The same 32^3 lattice with the iso value 0.5 that the benchmark's
+    configuration names.  ZB05's field is a distance minus the particle
+    radius, which on the narrow band (within 1.5h of the surface particles)
+    never reaches 0.5, so the frame has no valid cube and no triangle; every
+    stage still matches the oracle."""
+    from fluidsurfacereconstructiongpu_gb300 import synthetic
+    fr = synthetic.lattice_cube(32, 0.0125, seed=1)
+    rep = _run("zb05", fr, grid_ratio=8, iso=0.5)
+    assert rep["triangles"] == 0
