@@ -23,7 +23,6 @@
 #include "backward.h"
 
 #include <algorithm>
-#include <cstddef>
 
 namespace fsr {
 namespace {
@@ -188,7 +187,6 @@ struct WarpSlice {
     float psum[kPassTiles][32];  // per tile and lane: sum over the involved candidates
     float usum[kPassTiles][32];  // and over the non-involved ones
     uint16_t order[kPassVerts];  // the pass's vertices in brick order (tile t: entries 32t .. 32t+31)
-    uint16_t clist[32];          // the current tile's kept candidates, in order: byte offsets of their records in rec
     float mom[kMoments];         // moments of the group's non-involved candidates (unscaled_moments)
     uint32_t use_mom;            // the moment form applies to this group
     uint32_t cstart[128];
@@ -198,7 +196,6 @@ struct WarpSlice {
     uint32_t total_inv;          // candidates of involved cells (they come first)
     uint32_t ninv_cells;         // and the number of those cells
 };
-static_assert(offsetof(WarpSlice, clist) % 4 == 0, "clist is read two entries at a time");
 
 // The window cells of candidates cb .. cb + 31 of a sweep through the
 // tables, one per lane, from the table boundaries that fall inside the
@@ -671,14 +668,7 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
 #pragma unroll 1
                     for (int t = 0; t < kPassTiles; ++t) {
                         if ((uint32_t)t < ntiles) {
-                            // the candidates whose support sphere reaches the
-                            // tile, listed in order as byte offsets of their
-                            // records (one shared load per two of them in the
-                            // loop below instead of a bit scan of the mask)
-                            const bool r = keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]);
-                            const uint32_t m = __ballot_sync(0xffffffffu, r);
-                            if (r) w.clist[__popc(m & ((1u << lane) - 1u))] = (uint16_t)(lane * 3 * sizeof(float4));
-                            __syncwarp();
+                            const uint32_t m = __ballot_sync(0xffffffffu, keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]));
                             const uint32_t v = 32 * t + lane;
                             if (m && v < nv) {
                                 const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
@@ -691,17 +681,15 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
                                 float s = 0.f;
                                 // two kept candidates per step, evaluated without
                                 // branches; their terms enter the sum in order
-                                const int cnt = __popc(m);
-                                const unsigned char* recb = reinterpret_cast<const unsigned char*>(w.rec);
-                                for (int i = 0; i < cnt; i += 2) {
-                                    // entries i and i + 1 (the latter unused, and
-                                    // possibly stale, when i + 1 == cnt)
-                                    const uint32_t pr = *reinterpret_cast<const uint32_t*>(w.clist + i);
-                                    const bool two = i + 1 < cnt;
-                                    const uint32_t oa = pr & 0xffffu, ob = two ? pr >> 16 : oa;
+                                for (uint32_t mm = m; mm;) {
+                                    const int ka = __ffs(mm) - 1;
+                                    mm &= mm - 1u;
+                                    const bool two = mm != 0u;
+                                    const int kb = two ? __ffs(mm) - 1 : ka;
+                                    mm &= two ? mm - 1u : ~0u;
                                     float ua, ub, ca, cb;
-                                    const bool ina = term(reinterpret_cast<const float4*>(recb + oa), vp, ua, ca);
-                                    const bool inb = term(reinterpret_cast<const float4*>(recb + ob), vp, ub, cb);
+                                    const bool ina = term(w.rec + 3 * ka, vp, ua, ca);
+                                    const bool inb = term(w.rec + 3 * kb, vp, ub, cb);
                                     if (ina) s = fmaf(ca, ua, s);
                                     if (two && inb) s = fmaf(cb, ub, s);
                                 }
@@ -711,7 +699,6 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
                                 w.psum[t][lane] = t0;
                                 w.usum[t][lane] += (a0 - (t0 - bp)) + (s - bp);
                             }
-                            __syncwarp();  // the next tile rewrites clist
                         }
                     }
                 }
