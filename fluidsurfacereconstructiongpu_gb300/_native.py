@@ -48,6 +48,11 @@ class FrameHeader(ctypes.Structure):
                 ("particle_radius", c_f32), ("particle_mass", c_f32)]
 
 
+class HostFrame(ctypes.Structure):
+    _fields_ = [("header", FrameHeader), ("xyz", c_vp), ("density", c_vp), ("n", c_u64), ("out_pos", c_vp),
+                ("out_nrm", c_vp), ("capacity", c_u64), ("n_vertices", c_u64), ("status", ctypes.c_int)]
+
+
 class PairCounts(ctypes.Structure):
     _fields_ = [("smooth_candidates", c_u64), ("smooth_contributing", c_u64), ("cov_candidates", c_u64),
                 ("cov_contributing", c_u64), ("field_candidates", c_u64), ("field_contributing", c_u64),
@@ -110,6 +115,7 @@ def _load():
         "fsr_reconstruct": (ctypes.c_int, [c_vp, P(FrameHeader), c_vp, c_vp, c_u64, c_vp]),
         "fsr_reconstruct_host": (ctypes.c_int, [c_vp, P(FrameHeader), c_vp, c_vp, c_u64, c_vp, c_vp, c_u64,
                                                 P(c_u64), c_vp]),
+        "fsr_reconstruct_host_frames": (ctypes.c_int, [c_vp, P(HostFrame), c_u32, c_vp]),
         "fsr_mesh_device": (ctypes.c_int, [c_vp, P(c_vp), P(c_vp), P(c_u64)]),
         "fsr_copy_mesh": (ctypes.c_int, [c_vp, c_vp, c_vp, c_u64, P(c_u64)]),
         "fsr_get_stats": (ctypes.c_int, [c_vp, P(Stats)]),

@@ -156,6 +156,50 @@ class Reconstructor:
         N.check(st, self._h)
         return Mesh(pos[:nv.value], nrm[:nv.value])
 
+    def reconstruct_host_frames(self, frames, capacity: Optional[int] = None, stream=None):
+        """A sequence of frames, host memory in and out, with each frame's
+        upload and read-back overlapped with its neighbours' reconstruction
+        (fsr_reconstruct_host_frames).  `frames`: (xyz, density, header)
+        triples.  Returns one Mesh per frame; raises on the first failing
+        frame.  `capacity` (mesh vertices per frame) defaults to a bound from
+        the grid: pass the expected size to keep the pinned outputs small."""
+        import torch
+        ins, outs = [], []
+        arr = (N.HostFrame * len(frames))()
+        for k, (xyz, density, header) in enumerate(frames):
+            xyz = torch.from_numpy(np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)).pin_memory()
+            den = torch.from_numpy(np.ascontiguousarray(density, dtype=np.float32).reshape(-1)).pin_memory()
+            n = xyz.shape[0]
+            cap = int(capacity) if capacity is not None else max(4096, 24 * n)
+            pos = torch.empty((cap, 3), dtype=torch.float32).pin_memory()
+            nrm = torch.empty((cap, 3), dtype=torch.float32).pin_memory()
+            ins.append((xyz, den))
+            outs.append((pos, nrm))
+            arr[k].header = header
+            arr[k].xyz = xyz.data_ptr()
+            arr[k].density = den.data_ptr()
+            arr[k].n = n
+            arr[k].out_pos = pos.data_ptr()
+            arr[k].out_nrm = nrm.data_ptr()
+            arr[k].capacity = cap
+        st = N.lib.fsr_reconstruct_host_frames(self._h, arr, len(frames),
+                                               None if stream is None else ctypes.c_void_p(stream))
+        if st not in (0, 7):
+            N.check(st, self._h)
+        out = []
+        for k in range(len(frames)):
+            nv = arr[k].n_vertices
+            if arr[k].status == 7:  # outputs too small: this frame again on its own, sized by the call
+                xyz, den = ins[k]
+                out.append(self.reconstruct_host(xyz.numpy(), den.numpy(), frames[k][2]))
+            else:
+                N.check(arr[k].status, self._h)
+                out.append(Mesh(outs[k][0][:nv].numpy().copy(), outs[k][1][:nv].numpy().copy()))
+        if st == 7 and arr[len(frames) - 1].status == 0:  # the handle holds the last frame again
+            xyz, den = ins[-1]
+            self.reconstruct_host(xyz.numpy(), den.numpy(), frames[-1][2])
+        return out
+
     def mesh(self) -> Mesh:
         nv = int(self.stats().n_mesh_vertices)
         pos = np.empty((max(nv, 1), 3), np.float32)

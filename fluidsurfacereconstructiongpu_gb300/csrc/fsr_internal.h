@@ -17,7 +17,7 @@ namespace fsr {
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
-    cudaError_t ensure(size_t want);  // contents are not preserved on growth
+    cudaError_t ensure(size_t want);  // contents are not preserved on growth; growth waits for the device
     void release();
 };
 
@@ -89,6 +89,12 @@ struct fsr_handle {
     uint64_t launches_mark = 0;
     uint32_t launches_frame = 0;
     fsr::Counters* pinned_ctr = nullptr;
+    // fsr_reconstruct_host_frames: the second input and mesh buffers and
+    // counters, the copy streams and their events (created on first use)
+    fsr::DevBuf in_xyz_b, in_den_b, mesh_pos_b, mesh_nrm_b;
+    fsr::Counters* pinned_ctr_b = nullptr;
+    cudaStream_t up = nullptr, down = nullptr;
+    cudaEvent_t ev_up[2] = {}, ev_done[2] = {}, ev_down[2] = {};
     cudaEvent_t ev_start = nullptr;
     cudaEvent_t ev[FSR_NUM_STAGES] = {};
 

@@ -140,7 +140,13 @@ struct DeviceGuard {
 cudaError_t DevBuf::ensure(size_t want)
 {
     if (want <= bytes) return cudaSuccess;
-    if (ptr) cudaFree(ptr);
+    // the old block may still be read by work queued on another stream (a
+    // pipelined sequence uploads and downloads beside the kernels): let the
+    // device finish it before the block is freed
+    if (ptr) {
+        cudaDeviceSynchronize();
+        cudaFree(ptr);
+    }
     ptr = nullptr;
     bytes = 0;
     const size_t b = std::max<size_t>(want, 256);
@@ -165,9 +171,17 @@ fsr_handle::~fsr_handle()
     DeviceGuard g(device);
     for (DevBuf* b : all_buffers()) b->release();
     if (pinned_ctr) cudaFreeHost(pinned_ctr);
+    if (pinned_ctr_b) cudaFreeHost(pinned_ctr_b);
     for (auto& e : ev) {
         if (e) cudaEventDestroy(e);
     }
+    for (int k = 0; k < 2; ++k) {
+        if (ev_up[k]) cudaEventDestroy(ev_up[k]);
+        if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+        if (ev_down[k]) cudaEventDestroy(ev_down[k]);
+    }
+    if (up) cudaStreamDestroy(up);
+    if (down) cudaStreamDestroy(down);
     if (ev_start) cudaEventDestroy(ev_start);
 }
 
@@ -175,7 +189,7 @@ std::vector<DevBuf*> fsr_handle::all_buffers()
 {
     return {&in_xyz, &in_den,  &keys0,  &vals0,  &keys1, &vals1,  &radix_tmp, &sorted, &ranges,  &occ,
             &surf,   &invol, &cell_rmax,   &psurf,  &bits,   &prefix, &gflag, &glist, &scan_tmp, &sv,       &phi,    &mc,      &vofs,
-            &valid,   &mean,   &mean32, &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gklist, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri};
+            &valid,   &mean,   &mean32, &smoothed, &grec, &qrec, &covrec, &mesh_pos, &mesh_nrm, &wkey, &wslot, &wrank, &widx, &wpos, &wnrm, &wtable_keys, &wtable_first, &rho, &pflags, &ctr, &mv, &gphi, &gkey, &gklist, &gsmooth, &gG, &gmean, &gx, &gscalar, &tri, &in_xyz_b, &in_den_b, &mesh_pos_b, &mesh_nrm_b};
 }
 
 // ------------------------------------------------------------ frame

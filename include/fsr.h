@@ -152,6 +152,35 @@ fsr_status fsr_reconstruct_host(fsr_handle* h, const fsr_frame_header* hdr, cons
                                 const float* density, uint64_t n, float* out_pos, float* out_nrm,
                                 uint64_t capacity, uint64_t* n_vertices, void* stream);
 
+/* A sequence of frames from host memory to host memory (the reference's
+ * frame loop, ReconstructorGPU.cpp:25-79: per frame beginFrame uploads the
+ * particles, frameMove reconstructs, endFrame downloads the mesh, each
+ * stage followed by a device synchronisation).  Frame i + 1's particles are
+ * uploaded and frame i - 1's triangle soup is read back on two copy streams
+ * while frame i is reconstructed on `stream`, through a second input and a
+ * second mesh buffer of the handle.  Every frame gives exactly the results
+ * of fsr_reconstruct_host on the same particles; on return the handle holds
+ * the last frame (stats, mesh, intermediates for fsr_backward).  Stage
+ * timing (FSR_FLAG_STAGE_TIMING) is not recorded.  Each frame's status and
+ * vertex count are set; a frame whose mesh exceeds its capacity gets
+ * FSR_ERR_CAPACITY and the others still run.  Returns FSR_OK, or the first
+ * failing frame's status (an error other than FSR_ERR_CAPACITY stops the
+ * sequence; the frames after it keep FSR_ERR_NOT_READY).  Pinned host
+ * buffers let the copies overlap the reconstruction. */
+typedef struct fsr_host_frame {
+    fsr_frame_header header;
+    const float* xyz;      /* n x 3 */
+    const float* density;  /* n (not read with FSR_FLAG_COMPUTE_DENSITY) */
+    uint64_t n;
+    float* out_pos;        /* capacity x 3 */
+    float* out_nrm;        /* capacity x 3 */
+    uint64_t capacity;     /* mesh vertices the outputs hold */
+    uint64_t n_vertices;   /* out: mesh vertices of the frame */
+    fsr_status status;     /* out */
+} fsr_host_frame;
+
+fsr_status fsr_reconstruct_host_frames(fsr_handle* h, fsr_host_frame* frames, uint32_t count, void* stream);
+
 /* Device pointers to the last frame's mesh (valid until the next frame). */
 fsr_status fsr_mesh_device(fsr_handle* h, const float** d_pos, const float** d_nrm,
                            uint64_t* n_vertices);
