@@ -951,6 +951,73 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
     }
 }
 
+// The group box's vertices with a non-zero dL/dphi, listed in 4 x 4 x 2
+// bricks of the box, so that each 32 consecutive ones (which share one
+// culling box in the ZB05/TC01 adjoint) lie close together: a count per brick, a scan,
+// then a scatter (the order inside a brick is that of the atomics; it changes
+// no sum but the float atomics' order, which is not fixed anyway).
+// emit(slot, lx, ly, lz, rank, gv) stores one vertex (slots below `cap` only);
+// hist holds `cap` words.  Every thread of the block calls it; returns the
+// number of such vertices.
+template <class Emit>
+__device__ uint32_t list_grad_vertices(const BandView& band, const float* __restrict__ gphi, uint32_t nb,
+                                       const Grid& sc, const int lo[3], const int hi[3], uint32_t* hist, uint32_t cap,
+                                       uint32_t* s_tot, Emit&& emit)
+{
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
+    const int nbox = nx * ny * nz;
+    const int bx = (nx + 3) / 4, by = (ny + 3) / 4, bz = (nz + 1) / 2;
+    const bool bricks = (uint32_t)(bx * by * bz) <= cap;  // (always, for boxes within the capacity)
+    const int nbins = bricks ? bx * by * bz : 1;
+    auto key = [&](int lx, int ly, int lz) { return bricks ? (lx >> 2) + bx * ((ly >> 2) + by * (lz >> 1)) : 0; };
+    auto grad = [&](int i, int& lx, int& ly, int& lz, uint32_t& rank) -> float {
+        lx = i % nx;
+        ly = (i / nx) % ny;
+        lz = i / (nx * ny);
+        const uint32_t v = lin3(lo[0] + lx, lo[1] + ly, lo[2] + lz, sc);
+        if (!band_has(band, v)) return 0.f;
+        rank = band_rank(band, v);
+        return rank < nb ? __ldg(gphi + rank) : 0.f;
+    };
+    for (int b = tid; b < nbins; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
+    for (int i = tid; i < nbox; i += blockDim.x) {
+        int lx, ly, lz;
+        uint32_t rank = 0;
+        if (grad(i, lx, ly, lz, rank) != 0.f) atomicAdd(&hist[key(lx, ly, lz)], 1u);
+    }
+    __syncthreads();
+    if (tid < 32) {  // exclusive scan of the counts
+        uint32_t run = 0;
+        for (int b0 = 0; b0 < nbins; b0 += 32) {
+            const int b = b0 + lane;
+            const uint32_t cnt = b < nbins ? hist[b] : 0u;
+            uint32_t x = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (b < nbins) hist[b] = run + x - cnt;
+            run += __shfl_sync(0xffffffffu, x, 31);
+        }
+        if (lane == 0) *s_tot = run;
+    }
+    __syncthreads();
+    for (int i = tid; i < nbox; i += blockDim.x) {
+        int lx, ly, lz;
+        uint32_t rank = 0;
+        const float gv = grad(i, lx, ly, lz, rank);
+        if (gv != 0.f) {
+            const uint32_t slot = atomicAdd(&hist[key(lx, ly, lz)], 1u);
+            if (slot < cap) emit(slot, lx, ly, lz, rank, gv);
+        }
+    }
+    __syncthreads();
+    return *s_tot;
+}
+
 // ---------------------------------------------------------------- adjoint
 // dL/dx~ and dL/dG of the anisotropic field, grouped like the forward pass
 // but with the roles swapped: the group's band vertices that carry a
@@ -1021,7 +1088,8 @@ __global__ void k_field_aniso_backward_grouped(BwdGroupArgs a, uint32_t ratio, c
         const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
         const int nbox = nx * ny * nz;
 
-        // 1. the group's vertices with dL/dphi != 0
+        // 1. the group's vertices with dL/dphi != 0 (listed in scan order:
+        // brick order, as in the ZB05 adjoint, measured slower here)
         if (tid == 0) {
             s_nv = 0;
             s_next = 0;
@@ -1188,8 +1256,11 @@ __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, u
 {
     extern __shared__ __align__(16) unsigned char smem[];
     float4* av = reinterpret_cast<float4*>(smem);  // active vertices: (v, dL/dphi)
-    float4* am = av + vlist_cap;                    // ZB05: (mean - v, weight sum)
+    // ZB05, per active vertex: e = (mean - v) dL/dphi / (|mean - v| W) and e.(mean - v), so that a pair
+    // needs no square root or division (W: the weight sum; vertices without weight get 0)
+    float4* am = av + vlist_cap;
     float4* cbox = am + (TC01 ? 0 : vlist_cap);     // per 32 of them: lo, hi
+    uint32_t* hist = reinterpret_cast<uint32_t*>(cbox + 2 * ((vlist_cap + 31) / 32));  // vlist_cap words
     __shared__ uint32_t s_nv, s_rb[9], s_re[9], s_rp[10], s_next;
     const uint32_t nb = min(ctr->n_band, a.cap_band);
     const int tid = threadIdx.x, lane = tid & 31;
@@ -1210,43 +1281,23 @@ __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, u
         const uint32_t g = a.glist[4 + k];
         int c[3], lo[3], hi[3];
         if (!group_box(g, a.sp, a.sc, a.ratio, c, lo, hi)) continue;
-        const int nx = hi[0] - lo[0], ny = hi[1] - lo[1], nz = hi[2] - lo[2];
-        const int nbox = nx * ny * nz;
-        if (tid == 0) {
-            s_nv = 0;
-            s_next = 0;
-        }
-        __syncthreads();
-        for (int base = 0; base < nbox; base += kBT) {
-            const int i = base + tid;
-            float gv = 0.f;
-            uint32_t rank = 0;
-            int lx = 0, ly = 0, lz = 0;
-            if (i < nbox) {
-                lx = i % nx;
-                ly = (i / nx) % ny;
-                lz = i / (nx * ny);
-                const uint32_t v = lin3(lo[0] + lx, lo[1] + ly, lo[2] + lz, a.sc);
-                if (band_has(a.band, v)) {
-                    rank = band_rank(a.band, v);
-                    if (rank < nb) gv = __ldg(a.gphi + rank);
+        if (tid == 0) s_next = 0;
+        list_grad_vertices(a.band, a.gphi, nb, a.sc, lo, hi, hist, vlist_cap, &s_nv,
+                           [&](uint32_t slot, int lx, int ly, int lz, uint32_t rank, float gv) {
+            av[slot] = make_float4(vpos1(lo[0] + lx, a.sc.min[0], a.sc.cs), vpos1(lo[1] + ly, a.sc.min[1], a.sc.cs),
+                                   vpos1(lo[2] + lz, a.sc.min[2], a.sc.cs), gv);
+            if (!TC01) {
+                const float4 m = __ldg(a.mv + rank);  // mean - v, weight sum
+                const float ml = sqrtf(fmaf(m.x, m.x, fmaf(m.y, m.y, m.z * m.z)));
+                float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (m.w > 0.f && ml > 0.f) {
+                    const float f = gv / ml / m.w;
+                    e = make_float4(m.x * f, m.y * f, m.z * f, 0.f);
+                    e.w = fmaf(e.x, m.x, fmaf(e.y, m.y, e.z * m.z));
                 }
+                am[slot] = e;
             }
-            const bool act = gv != 0.f;
-            const uint32_t m = __ballot_sync(0xffffffffu, act);
-            uint32_t off = 0;
-            if (lane == 0 && m) off = atomicAdd(&s_nv, __popc(m));
-            off = __shfl_sync(0xffffffffu, off, 0);
-            if (act) {
-                const uint32_t slot = off + __popc(m & ((1u << lane) - 1u));
-                if (slot < vlist_cap) {
-                    av[slot] = make_float4(vpos1(lo[0] + lx, a.sc.min[0], a.sc.cs),
-                                           vpos1(lo[1] + ly, a.sc.min[1], a.sc.cs),
-                                           vpos1(lo[2] + lz, a.sc.min[2], a.sc.cs), gv);
-                    if (!TC01) am[slot] = __ldg(a.mv + rank);
-                }
-            }
-        }
+        });
         // the +-1 window's rows (x-adjacent cells are contiguous in the sorted order)
         if (tid < 9) {
             const int x0 = clampi(c[0] - 1, 0, (int)a.sp.res[0] - 1), x1 = clampi(c[0] + 1, 0, (int)a.sp.res[0] - 1);
@@ -1319,22 +1370,17 @@ __global__ void __launch_bounds__(kBT) k_field_iso_backward_grouped(BwdArgs a, u
                         gz = fmaf(sg, dz, gz);
                     } else {
                         if (d2 >= h2) continue;
-                        const float4 m = am[t];  // mean - v, weight sum
-                        if (!(m.w > 0.f)) continue;
-                        const float ml = sqrtf(fmaf(m.x, m.x, fmaf(m.y, m.y, m.z * m.z)));
-                        if (!(ml > 0.f)) continue;
+                        const float4 e = am[t];
                         const float u = 1.0f - d2 * inv_h2;
                         const float wt = u * u * u;
                         // d phi / d xbar = (xbar - v) / |xbar - v|; d xbar / d x_j = (w I + (x_j - xbar)
-                        // (dw/dx_j)^T) / W with dw/dx_j = -6 u^2 (x_j - v) / h^2
-                        const float il = v.w / ml;
-                        const float ex = m.x * il, ey = m.y * il, ez = m.z * il;
-                        const float proj = ex * (dx - m.x) + ey * (dy - m.y) + ez * (dz - m.z);
-                        const float k2 = proj * (-6.0f * u * u * inv_h2);
-                        const float iw = 1.0f / m.w;
-                        gx += (wt * ex + k2 * dx) * iw;
-                        gy += (wt * ey + k2 * dy) * iw;
-                        gz += (wt * ez + k2 * dz) * iw;
+                        // (dw/dx_j)^T) / W with dw/dx_j = -6 u^2 (x_j - v) / h^2; with e as above
+                        // (x_j - xbar = d - (mean - v)):
+                        //   dL/dx_j += wt e + (e.d - e.(mean - v)) (-6 u^2 / h^2) d
+                        const float k2 = (fmaf(e.x, dx, fmaf(e.y, dy, e.z * dz)) - e.w) * (-6.0f * u * u * inv_h2);
+                        gx = fmaf(wt, e.x, fmaf(k2, dx, gx));
+                        gy = fmaf(wt, e.y, fmaf(k2, dy, gy));
+                        gz = fmaf(wt, e.z, fmaf(k2, dz, gz));
                     }
                 }
             }
@@ -1411,7 +1457,8 @@ void launch_field_aniso_grouped(const KernelCtx& c, const AnisoFieldArgs& f, con
 bool launch_field_iso_backward_grouped(const KernelCtx& c, const BwdArgs& a, bool tc01, const Counters* ctr)
 {
     const uint32_t vcap = (a.ratio + 2) * (a.ratio + 2) * (a.ratio + 2);
-    const size_t smem = sizeof(float4) * vcap * (tc01 ? 1 : 2) + sizeof(float4) * 2 * ((vcap + 31) / 32);
+    const size_t smem = sizeof(float4) * vcap * (tc01 ? 1 : 2) + sizeof(float4) * 2 * ((vcap + 31) / 32) +
+                        sizeof(uint32_t) * vcap;
     if (smem > 200 * 1024) return false;
     static bool configured = false;
     if (!configured) {
