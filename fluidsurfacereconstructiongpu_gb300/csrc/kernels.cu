@@ -977,17 +977,30 @@ __device__ __forceinline__ void normalize_guarded(float n[3])
 // generateTriangles (cu:383-463), or with host_mc the host marching cubes
 // of Akinci12 (MarchingCubesCPU.cpp:3-72: no normal sign flip, guarded
 // normalisation, epsilon test in double).
+// The 32 grid positions a cube's corners and central-difference normals
+// read: for each corner row (y, z in {0,1}) x = -1..2 (slots 0-15, the
+// corners at x = 0, 1), and above/below each corner column y = -1, 2
+// (slots 16-23) and z = -1, 2 (slots 24-31).  Each slot outside the cube
+// serves one corner's normal, so that normal is written back over its three
+// such slots once it is formed.
+__device__ __forceinline__ int mc_corner_slot(int cx, int cy, int cz) { return (cz * 2 + cy) * 4 + cx + 1; }
+__device__ __forceinline__ int mc_nx_slot(int cx, int cy, int cz) { return (cz * 2 + cy) * 4 + (cx ? 3 : 0); }
+__device__ __forceinline__ int mc_ny_slot(int cx, int cy, int cz) { return 16 + (cz * 2 + cx) * 2 + cy; }
+__device__ __forceinline__ int mc_nz_slot(int cx, int cy, int cz) { return 24 + (cy * 2 + cx) * 2 + cz; }
+
 __global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counters* ctr)
 {
-    // corner values and normals per thread in shared memory ([corner][thread]),
-    // so that the cut edges can index them without spilling registers
-    __shared__ float s_val[8 * kThreads];
-    __shared__ float s_nrm[24 * kThreads];
+    // per thread: the cube's 32 field values, then corner values and normals
+    // ([slot][thread]), so that the cut edges can index them without
+    // spilling registers
+    __shared__ float s_f[32 * kThreads];
     const uint32_t nq = min(ctr->n_valid, a.cap_valid);
     const uint32_t ntot = ctr->n_mesh_verts;
     if (ntot > a.cap_mesh) return;
     const float sgn = a.host_mc ? 1.0f : (a.iso < 0.0f ? -1.0f : 1.0f);
     const int tid = threadIdx.x;
+    float* f = s_f + tid;
+    auto S = [&](int slot) -> float& { return f[slot * kThreads]; };
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
         const uint32_t t = a.valid[q];
         const uint32_t info = a.mc[t];
@@ -996,23 +1009,42 @@ __global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counte
         const uint32_t base = a.vofs[t];
         uint32_t x, y, z;
         unlin3(a.sv[t], a.sc, x, y, z);
+        const int X = (int)x, Y = (int)y, Z = (int)z;
+        // the 32 positions, each looked up once (the corner-by-corner form
+        // reads 56)
+        for (int r = 0; r < 4; ++r) {
+            const int cy = r & 1, cz = r >> 1;
+            for (int xi = 0; xi < 4; ++xi) S(r * 4 + xi) = field_at(a, X + xi - 1, Y + cy, Z + cz);
+        }
+        for (int k = 0; k < 4; ++k) {
+            const int c0 = k & 1, c1 = k >> 1;
+            S(16 + k * 2) = field_at(a, X + c0, Y - 1, Z + c1);      // (cx, cz) = (c0, c1)
+            S(16 + k * 2 + 1) = field_at(a, X + c0, Y + 2, Z + c1);
+            S(24 + k * 2) = field_at(a, X + c0, Y + c1, Z - 1);      // (cx, cy) = (c0, c1)
+            S(24 + k * 2 + 1) = field_at(a, X + c0, Y + c1, Z + 2);
+        }
+        // corner normals, f(p - e) - f(p + e) per axis, over their slots
         for (int i = 0; i < 8; ++i) {
-            const int cx = (int)x + mc::cornerDx(i), cy = (int)y + mc::cornerDy(i), cz = (int)z + mc::cornerDz(i);
-            s_val[i * kThreads + tid] = field_at(a, cx, cy, cz);
-            float cn[3] = {field_at(a, cx - 1, cy, cz) - field_at(a, cx + 1, cy, cz),
-                           field_at(a, cx, cy - 1, cz) - field_at(a, cx, cy + 1, cz),
-                           field_at(a, cx, cy, cz - 1) - field_at(a, cx, cy, cz + 1)};
+            const int cx = mc::cornerDx(i), cy = mc::cornerDy(i), cz = mc::cornerDz(i);
+            float cn[3] = {cx ? S(mc_corner_slot(0, cy, cz)) - S(mc_nx_slot(1, cy, cz))
+                              : S(mc_nx_slot(0, cy, cz)) - S(mc_corner_slot(1, cy, cz)),
+                           cy ? S(mc_corner_slot(cx, 0, cz)) - S(mc_ny_slot(cx, 1, cz))
+                              : S(mc_ny_slot(cx, 0, cz)) - S(mc_corner_slot(cx, 1, cz)),
+                           cz ? S(mc_corner_slot(cx, cy, 0)) - S(mc_nz_slot(cx, cy, 1))
+                              : S(mc_nz_slot(cx, cy, 0)) - S(mc_corner_slot(cx, cy, 1))};
             if (a.host_mc) normalize_guarded(cn);
             else normalize_fast(cn);
-            s_nrm[(3 * i) * kThreads + tid] = cn[0];
-            s_nrm[(3 * i + 1) * kThreads + tid] = cn[1];
-            s_nrm[(3 * i + 2) * kThreads + tid] = cn[2];
+            S(mc_nx_slot(cx, cy, cz)) = cn[0];
+            S(mc_ny_slot(cx, cy, cz)) = cn[1];
+            S(mc_nz_slot(cx, cy, cz)) = cn[2];
         }
         const uint64_t tri = c_mc.tri[cs];
         for (uint32_t k = 0; k < nv; ++k) {
             const int e = (int)((tri >> (4u * k)) & 0xFu);
             const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
-            const float v0 = s_val[i0 * kThreads + tid], v1 = s_val[i1 * kThreads + tid];
+            const int a0x = mc::cornerDx(i0), a0y = mc::cornerDy(i0), a0z = mc::cornerDz(i0);
+            const int a1x = mc::cornerDx(i1), a1y = mc::cornerDy(i1), a1z = mc::cornerDz(i1);
+            const float v0 = S(mc_corner_slot(a0x, a0y, a0z)), v1 = S(mc_corner_slot(a1x, a1y, a1z));
             const float d = v1 - v0;
             const float f = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - v0) / d;
             const int c0[3] = {(int)x + mc::cornerDx(i0), (int)y + mc::cornerDy(i0), (int)z + mc::cornerDz(i0)};
@@ -1022,7 +1054,10 @@ __global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counte
             for (int kk = 0; kk < 3; ++kk) {
                 const float p0 = vpos1(c0[kk], a.sc.min[kk], a.sc.cs), p1 = vpos1(c1[kk], a.sc.min[kk], a.sc.cs);
                 ip[kk] = fmaf(f, p1 - p0, p0);
-                const float n0 = s_nrm[(3 * i0 + kk) * kThreads + tid], n1 = s_nrm[(3 * i1 + kk) * kThreads + tid];
+                const float n0 = S(kk == 0 ? mc_nx_slot(a0x, a0y, a0z) : kk == 1 ? mc_ny_slot(a0x, a0y, a0z)
+                                                                       : mc_nz_slot(a0x, a0y, a0z));
+                const float n1 = S(kk == 0 ? mc_nx_slot(a1x, a1y, a1z) : kk == 1 ? mc_ny_slot(a1x, a1y, a1z)
+                                                                       : mc_nz_slot(a1x, a1y, a1z));
                 in[kk] = fmaf(f, n1 - n0, n0);
             }
             if (a.host_mc) normalize_guarded(in);
