@@ -998,71 +998,106 @@ __global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counte
     const uint32_t ntot = ctr->n_mesh_verts;
     if (ntot > a.cap_mesh) return;
     const float sgn = a.host_mc ? 1.0f : (a.iso < 0.0f ? -1.0f : 1.0f);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wbase = tid & ~31;
     float* f = s_f + tid;
     auto S = [&](int slot) -> float& { return f[slot * kThreads]; };
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        const uint32_t t = a.valid[q];
-        const uint32_t info = a.mc[t];
-        const uint32_t cs = info >> 8;
-        const uint32_t nv = info & 0xFFu;
-        const uint32_t base = a.vofs[t];
-        uint32_t x, y, z;
-        unlin3(a.sv[t], a.sc, x, y, z);
-        const int X = (int)x, Y = (int)y, Z = (int)z;
-        // the 32 positions, each looked up once (the corner-by-corner form
-        // reads 56)
-        for (int r = 0; r < 4; ++r) {
-            const int cy = r & 1, cz = r >> 1;
-            for (int xi = 0; xi < 4; ++xi) S(r * 4 + xi) = field_at(a, X + xi - 1, Y + cy, Z + cz);
+    // a warp takes 32 consecutive valid cubes: their vertices are one
+    // contiguous run of the output, which the warp then writes with
+    // consecutive lanes on consecutive vertices (coalesced stores)
+    for (uint32_t q0 = blockIdx.x * blockDim.x + (uint32_t)wbase; q0 < nq; q0 += gridDim.x * blockDim.x) {
+        const uint32_t q = q0 + (uint32_t)lane;
+        uint32_t cs = 0, nv = 0, base = 0;
+        int X = 0, Y = 0, Z = 0;
+        if (q < nq) {
+            const uint32_t t = a.valid[q];
+            const uint32_t info = a.mc[t];
+            cs = info >> 8;
+            nv = info & 0xFFu;
+            base = a.vofs[t];
+            uint32_t x, y, z;
+            unlin3(a.sv[t], a.sc, x, y, z);
+            X = (int)x;
+            Y = (int)y;
+            Z = (int)z;
+            // the 32 positions, each looked up once (the corner-by-corner form
+            // reads 56)
+            for (int r = 0; r < 4; ++r) {
+                const int cy = r & 1, cz = r >> 1;
+                for (int xi = 0; xi < 4; ++xi) S(r * 4 + xi) = field_at(a, X + xi - 1, Y + cy, Z + cz);
+            }
+            for (int k = 0; k < 4; ++k) {
+                const int c0 = k & 1, c1 = k >> 1;
+                S(16 + k * 2) = field_at(a, X + c0, Y - 1, Z + c1);      // (cx, cz) = (c0, c1)
+                S(16 + k * 2 + 1) = field_at(a, X + c0, Y + 2, Z + c1);
+                S(24 + k * 2) = field_at(a, X + c0, Y + c1, Z - 1);      // (cx, cy) = (c0, c1)
+                S(24 + k * 2 + 1) = field_at(a, X + c0, Y + c1, Z + 2);
+            }
+            // corner normals, f(p - e) - f(p + e) per axis, over their slots
+            for (int i = 0; i < 8; ++i) {
+                const int cx = mc::cornerDx(i), cy = mc::cornerDy(i), cz = mc::cornerDz(i);
+                float cn[3] = {cx ? S(mc_corner_slot(0, cy, cz)) - S(mc_nx_slot(1, cy, cz))
+                                  : S(mc_nx_slot(0, cy, cz)) - S(mc_corner_slot(1, cy, cz)),
+                               cy ? S(mc_corner_slot(cx, 0, cz)) - S(mc_ny_slot(cx, 1, cz))
+                                  : S(mc_ny_slot(cx, 0, cz)) - S(mc_corner_slot(cx, 1, cz)),
+                               cz ? S(mc_corner_slot(cx, cy, 0)) - S(mc_nz_slot(cx, cy, 1))
+                                  : S(mc_nz_slot(cx, cy, 0)) - S(mc_corner_slot(cx, cy, 1))};
+                if (a.host_mc) normalize_guarded(cn);
+                else normalize_fast(cn);
+                S(mc_nx_slot(cx, cy, cz)) = cn[0];
+                S(mc_ny_slot(cx, cy, cz)) = cn[1];
+                S(mc_nz_slot(cx, cy, cz)) = cn[2];
+            }
         }
-        for (int k = 0; k < 4; ++k) {
-            const int c0 = k & 1, c1 = k >> 1;
-            S(16 + k * 2) = field_at(a, X + c0, Y - 1, Z + c1);      // (cx, cz) = (c0, c1)
-            S(16 + k * 2 + 1) = field_at(a, X + c0, Y + 2, Z + c1);
-            S(24 + k * 2) = field_at(a, X + c0, Y + c1, Z - 1);      // (cx, cy) = (c0, c1)
-            S(24 + k * 2 + 1) = field_at(a, X + c0, Y + c1, Z + 2);
+        // the warp's run: the exclusive prefix of its cubes' vertex counts
+        uint32_t ex = nv;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, ex, o);
+            if (lane >= o) ex += y;
         }
-        // corner normals, f(p - e) - f(p + e) per axis, over their slots
-        for (int i = 0; i < 8; ++i) {
-            const int cx = mc::cornerDx(i), cy = mc::cornerDy(i), cz = mc::cornerDz(i);
-            float cn[3] = {cx ? S(mc_corner_slot(0, cy, cz)) - S(mc_nx_slot(1, cy, cz))
-                              : S(mc_nx_slot(0, cy, cz)) - S(mc_corner_slot(1, cy, cz)),
-                           cy ? S(mc_corner_slot(cx, 0, cz)) - S(mc_ny_slot(cx, 1, cz))
-                              : S(mc_ny_slot(cx, 0, cz)) - S(mc_corner_slot(cx, 1, cz)),
-                           cz ? S(mc_corner_slot(cx, cy, 0)) - S(mc_nz_slot(cx, cy, 1))
-                              : S(mc_nz_slot(cx, cy, 0)) - S(mc_corner_slot(cx, cy, 1))};
-            if (a.host_mc) normalize_guarded(cn);
-            else normalize_fast(cn);
-            S(mc_nx_slot(cx, cy, cz)) = cn[0];
-            S(mc_ny_slot(cx, cy, cz)) = cn[1];
-            S(mc_nz_slot(cx, cy, cz)) = cn[2];
-        }
-        const uint64_t tri = c_mc.tri[cs];
-        for (uint32_t k = 0; k < nv; ++k) {
-            const int e = (int)((tri >> (4u * k)) & 0xFu);
+        const uint32_t total = __shfl_sync(0xffffffffu, ex, 31);
+        ex -= nv;
+        const uint32_t run0 = __shfl_sync(0xffffffffu, base, 0);  // lane 0 holds a cube (q0 < nq)
+        __syncwarp();
+        for (uint32_t jb = 0; jb < total; jb += 32) {
+            const uint32_t j = jb + (uint32_t)lane;
+            // the cube of vertex j: the last lane whose run starts at or before j
+            int c = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xffffffffu, ex, (c + step) & 31);
+                if (c + step < 32 && e <= j) c += step;
+            }
+            const uint32_t k = j - __shfl_sync(0xffffffffu, ex, c);
+            const uint32_t ccs = __shfl_sync(0xffffffffu, cs, c);
+            const int cX = __shfl_sync(0xffffffffu, X, c), cY = __shfl_sync(0xffffffffu, Y, c),
+                      cZ = __shfl_sync(0xffffffffu, Z, c);
+            if (j >= total) continue;
+            const float* g = s_f + wbase + c;  // that cube's slots
+            auto G = [&](int slot) { return g[slot * kThreads]; };
+            const int e = (int)((c_mc.tri[ccs] >> (4u * k)) & 0xFu);
             const int i0 = mc::edgeA(e), i1 = mc::edgeB(e);
             const int a0x = mc::cornerDx(i0), a0y = mc::cornerDy(i0), a0z = mc::cornerDz(i0);
             const int a1x = mc::cornerDx(i1), a1y = mc::cornerDy(i1), a1z = mc::cornerDz(i1);
-            const float v0 = S(mc_corner_slot(a0x, a0y, a0z)), v1 = S(mc_corner_slot(a1x, a1y, a1z));
+            const float v0 = G(mc_corner_slot(a0x, a0y, a0z)), v1 = G(mc_corner_slot(a1x, a1y, a1z));
             const float d = v1 - v0;
-            const float f = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - v0) / d;
-            const int c0[3] = {(int)x + mc::cornerDx(i0), (int)y + mc::cornerDy(i0), (int)z + mc::cornerDz(i0)};
-            const int c1[3] = {(int)x + mc::cornerDx(i1), (int)y + mc::cornerDy(i1), (int)z + mc::cornerDz(i1)};
+            const float fr = (d > -1.0e-7f && d < 1.0e-7f) ? 0.5f : (a.iso - v0) / d;
+            const int c0[3] = {cX + a0x, cY + a0y, cZ + a0z};
+            const int c1[3] = {cX + a1x, cY + a1y, cZ + a1z};
             float ip[3], in[3];
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
                 const float p0 = vpos1(c0[kk], a.sc.min[kk], a.sc.cs), p1 = vpos1(c1[kk], a.sc.min[kk], a.sc.cs);
-                ip[kk] = fmaf(f, p1 - p0, p0);
-                const float n0 = S(kk == 0 ? mc_nx_slot(a0x, a0y, a0z) : kk == 1 ? mc_ny_slot(a0x, a0y, a0z)
+                ip[kk] = fmaf(fr, p1 - p0, p0);
+                const float n0 = G(kk == 0 ? mc_nx_slot(a0x, a0y, a0z) : kk == 1 ? mc_ny_slot(a0x, a0y, a0z)
                                                                        : mc_nz_slot(a0x, a0y, a0z));
-                const float n1 = S(kk == 0 ? mc_nx_slot(a1x, a1y, a1z) : kk == 1 ? mc_ny_slot(a1x, a1y, a1z)
+                const float n1 = G(kk == 0 ? mc_nx_slot(a1x, a1y, a1z) : kk == 1 ? mc_ny_slot(a1x, a1y, a1z)
                                                                        : mc_nz_slot(a1x, a1y, a1z));
-                in[kk] = fmaf(f, n1 - n0, n0);
+                in[kk] = fmaf(fr, n1 - n0, n0);
             }
             if (a.host_mc) normalize_guarded(in);
             else normalize_fast(in);
-            const uint64_t o = 3ull * (base + k);
+            const uint64_t o = 3ull * (run0 + j);
             a.out_pos[o] = ip[0];
             a.out_pos[o + 1] = ip[1];
             a.out_pos[o + 2] = ip[2];
@@ -1076,9 +1111,10 @@ __global__ void __launch_bounds__(kThreads) k_mc_generate(McArgs a, const Counte
                                lz = (uint32_t)min(c0[2], c1[2]);
                 const uint32_t axis = c0[0] != c1[0] ? 0u : (c0[1] != c1[1] ? 1u : 2u);
                 const uint64_t lin = (uint64_t)lx + (uint64_t)a.sc.res[0] * ((uint64_t)ly + (uint64_t)a.sc.res[1] * lz);
-                a.out_key[base + k] = 3ull * lin + axis;
+                a.out_key[run0 + j] = 3ull * lin + axis;
             }
         }
+        __syncwarp();  // the next cubes overwrite the slots
     }
 }
 
