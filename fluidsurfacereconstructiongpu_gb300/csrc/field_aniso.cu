@@ -806,6 +806,9 @@ __device__ __forceinline__ bool within(float4 q, float4 lo, float4 hi, float r2)
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r2;
 }
 
+#ifndef FSR_ISO_PAIRS
+#define FSR_ISO_PAIRS 1
+#endif
 template <bool TC01>
 __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandView band, uint32_t ratio, Counters* ctr)
 {
@@ -894,6 +897,42 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                 ay = w.sum[2][t][lane];
                                 az = w.sum[3][t][lane];
                             }
+#if FSR_ISO_PAIRS
+                            // two candidates per step, their terms added in order
+                            for (uint32_t mm = m; mm;) {
+                                const int ka = __ffs(mm) - 1;
+                                mm &= mm - 1u;
+                                const bool two = mm != 0u;
+                                const int kb = two ? __ffs(mm) - 1 : ka;
+                                mm &= two ? mm - 1u : ~0u;
+                                const float4 qa = w.rec[ka], qb = w.rec[kb];
+                                const float dxa = qa.x - vp.x, dya = qa.y - vp.y, dza = qa.z - vp.z;
+                                const float dxb = qb.x - vp.x, dyb = qb.y - vp.y, dzb = qb.z - vp.z;
+                                const float d2a = fmaf(dxa, dxa, fmaf(dya, dya, dza * dza));
+                                const float d2b = fmaf(dxb, dxb, fmaf(dyb, dyb, dzb * dzb));
+                                if (TC01) {
+                                    const float ua = d2a * a.inv_h2 * 0.5f, ub = d2b * a.inv_h2 * 0.5f;
+                                    const float ta = ua * ua - ua + 0.25f, tb = ub * ub - ub + 0.25f;
+                                    if (d2a <= a.h2) ws += ta;
+                                    if (two && d2b <= a.h2) ws += tb;
+                                } else {
+                                    const float ua = 1.0f - d2a * a.inv_h2, ub = 1.0f - d2b * a.inv_h2;
+                                    const float wa = ua * ua * ua, wb = ub * ub * ub;
+                                    if (d2a < a.h2) {
+                                        ws += wa;
+                                        ax = fmaf(dxa, wa, ax);
+                                        ay = fmaf(dya, wa, ay);
+                                        az = fmaf(dza, wa, az);
+                                    }
+                                    if (two && d2b < a.h2) {
+                                        ws += wb;
+                                        ax = fmaf(dxb, wb, ax);
+                                        ay = fmaf(dyb, wb, ay);
+                                        az = fmaf(dzb, wb, az);
+                                    }
+                                }
+                            }
+#else
                             for (uint32_t mm = m; mm; mm &= mm - 1u) {
                                 const float4 qq = w.rec[__ffs(mm) - 1];
                                 const float dx = qq.x - vp.x, dy = qq.y - vp.y, dz = qq.z - vp.z;
@@ -912,6 +951,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                     az = fmaf(dz, wt, az);
                                 }
                             }
+#endif
                             w.sum[0][t][lane] = ws;
                             if (!TC01) {
                                 w.sum[1][t][lane] = ax;
