@@ -791,6 +791,9 @@ __device__ __forceinline__ float field_at(const McArgs& a, int x, int y, int z)
     return r < a.cap_band ? __ldg(a.band.phi + r) : a.fill;  // r >= cap only in a frame that is re-run
 }
 
+#ifndef FSR_CLASSIFY_ROWS
+#define FSR_CLASSIFY_ROWS 1
+#endif
 // detectValidSurfaceCubes (cu:328-364): a band vertex as cube origin is
 // valid when all 8 corners are band vertices and the case emits triangles.
 __global__ void k_mc_classify(McArgs a, const Counters* ctr)
@@ -802,6 +805,43 @@ __global__ void k_mc_classify(McArgs a, const Counters* ctr)
         uint32_t x, y, z;
         unlin3(v, a.sc, x, y, z);
         uint32_t info = 0;
+#if FSR_CLASSIFY_ROWS
+        // the cube's corners as 4 rows of two x-neighbours, (dy, dz) in
+        // {0,1}^2: one bitset word (two when the pair straddles a word) and
+        // one prefix per row give both memberships and both ranks (the x + 1
+        // corner of a row in the band follows its x corner: rank + 1)
+        if (x < a.sc.res[0] - 1 && y < a.sc.res[1] - 1 && z < a.sc.res[2] - 1) {
+            uint32_t vr[4], wd[4];
+            bool all = true;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                vr[r] = v + (uint32_t)(r & 1) * rx + (uint32_t)(r >> 1) * rxy;
+                const uint32_t w = vr[r] >> 5, b = vr[r] & 31u;
+                wd[r] = __ldg(a.band.bits + w);
+                const uint32_t next = b < 31u ? (wd[r] >> (b + 1)) : __ldg(a.band.bits + w + 1);
+                all = all && ((wd[r] >> b) & 1u) && (next & 1u);
+            }
+            if (all) {
+                uint32_t cs = 0;
+                bool in_cap = true;
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const uint32_t b = vr[r] & 31u;
+                    const uint32_t r0 = r == 0 ? t : __ldg(a.band.prefix + (vr[r] >> 5)) + __popc(wd[r] & ((1u << b) - 1u));
+                    // ranks beyond the capacity only occur in a frame that overflowed and is re-run
+                    if (r0 + 1 >= a.cap_band) {
+                        in_cap = false;
+                        break;
+                    }
+                    const int dy = r & 1, dz = r >> 1;
+                    const int i0 = dy ? (dz ? 2 : 3) : (dz ? 1 : 0);  // corner (0, dy, dz); (1, dy, dz) is i0 + 4
+                    if (__ldg(a.band.phi + r0) <= a.iso) cs |= 1u << i0;
+                    if (__ldg(a.band.phi + r0 + 1) <= a.iso) cs |= 1u << (i0 + 4);
+                }
+                if (in_cap) info = (uint32_t)c_mc.nverts[cs] | (cs << 8);
+            }
+        }
+#else
         if (x < a.sc.res[0] - 1 && y < a.sc.res[1] - 1 && z < a.sc.res[2] - 1) {
             bool all = true;
             uint32_t ids[8];
@@ -827,6 +867,7 @@ __global__ void k_mc_classify(McArgs a, const Counters* ctr)
                 if (in_cap) info = (uint32_t)c_mc.nverts[cs] | (cs << 8);
             }
         }
+#endif
         a.mc[t] = info;
     }
 }
