@@ -71,6 +71,29 @@ __device__ __forceinline__ bool group_box(uint32_t g, const Grid& sp, const Grid
     return hi[0] > lo[0] && hi[1] > lo[1] && hi[2] > lo[2];
 }
 
+// Work items of the forward field kernels: a frame with few window groups
+// (a small frame) would leave most SMs idle with one warp per group, so each
+// group's vertex box is then cut into S slabs along z, each a work item of
+// its own (a vertex lies in one slab; a slab is listed, culled and summed
+// like a group).  S depends only on the number of groups, so a frame's
+// results do not depend on the launch shape.
+constexpr uint32_t kSlabTarget = 4096;  // work items wanted
+__device__ __forceinline__ uint32_t field_slabs(uint32_t ngroups)
+{
+    return ngroups >= kSlabTarget ? 1u : min(8u, (kSlabTarget + ngroups - 1) / max(ngroups, 1u));
+}
+// Restricts the box [lo, hi) to slab `part` of S along z; false when empty.
+__device__ __forceinline__ bool slab_box(uint32_t part, uint32_t S, int lo[3], int hi[3])
+{
+    if (S == 1) return true;
+    const uint32_t nz = (uint32_t)(hi[2] - lo[2]);
+    const int z0 = lo[2] + (int)(nz * part / S), z1 = lo[2] + (int)(nz * (part + 1) / S);
+    if (z0 >= z1) return false;
+    lo[2] = z0;
+    hi[2] = z1;
+    return true;
+}
+
 // Lists the candidate cells of the window around cell c (clamped as in the
 // reference, cu:856-864), dropping involved cells whose reach cannot touch
 // the box [b0, b1], and scans their particle counts.  Every thread of the
@@ -577,15 +600,16 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
     WarpSlice& w = slices[threadIdx.x >> 5];
     const uint32_t nb = min(ctr->n_band, a.cap);
     const uint32_t ngroups = ctr->n_groups;  // groups holding band vertices
+    const uint32_t nslab = field_slabs(ngroups);
 
     for (;;) {
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&ctr->work_field, 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= ngroups) break;
-        const uint32_t g = a.glist[k];
+        if (k >= ngroups * nslab) break;
+        const uint32_t g = a.glist[k / nslab];
         int c[3], lo[3], hi[3];
-        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
+        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi) || !slab_box(k % nslab, nslab, lo, hi)) continue;
         bool tables = false;
         uint32_t total = 0;
 
@@ -817,6 +841,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
     IsoSlice& w = slices[threadIdx.x >> 5];
     const uint32_t nb = min(ctr->n_band, a.cap);
     const uint32_t ngroups = ctr->n_groups;  // groups holding band vertices
+    const uint32_t nslab = field_slabs(ngroups);
     const float cr = cull_radius(a.h, a.sp.cs), cr2 = cr * cr;
     constexpr int kSums = TC01 ? 1 : 4;
 
@@ -824,10 +849,10 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&ctr->work_field, 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
-        if (k >= ngroups) break;
-        const uint32_t g = a.glist[k];
+        if (k >= ngroups * nslab) break;
+        const uint32_t g = a.glist[k / nslab];
         int c[3], lo[3], hi[3];
-        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi)) continue;
+        if (!group_box(g, a.sp, a.sc, ratio, c, lo, hi) || !slab_box(k % nslab, nslab, lo, hi)) continue;
         // rows of the +-1 window (clamped as window() clamps), z then y
         if (lane < 9) {
             const int x0 = clampi(c[0] - 1, 0, (int)a.sp.res[0] - 1), x1 = clampi(c[0] + 1, 0, (int)a.sp.res[0] - 1);
