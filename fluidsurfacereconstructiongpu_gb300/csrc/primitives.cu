@@ -129,6 +129,51 @@ uint32_t grid_for_tiles(uint64_t n_max)
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(t, 65535));
 }
 
+// One-block exclusive scan (in place allowed) for short arrays: tiles of
+// 4 x 1024 consecutive elements, each thread four of them, a block scan per
+// tile and a running carry.  One launch instead of three.
+constexpr uint32_t kSingleThreads = 1024;
+constexpr uint32_t kSingleMax = 1u << 14;  // longer arrays take the tiled three-kernel scan (one block is slower from ~64k on)
+__global__ void __launch_bounds__(kSingleThreads) k_scan_single(const uint32_t* in, uint32_t* out, uint32_t n)
+{
+    __shared__ uint32_t warp_sums[kSingleThreads / 32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < n; base += 4 * kSingleThreads) {
+        const uint32_t i0 = base + 4 * threadIdx.x;
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = i0 + k < n ? in[i0 + k] : 0u;
+        const uint32_t s = v[0] + v[1] + v[2] + v[3];
+        uint32_t x = s;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+#pragma unroll
+            for (uint32_t o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        uint32_t run = carry + x - s + (warp ? warp_sums[warp - 1] : 0u);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) out[i0 + k] = run;
+            run += v[k];
+        }
+        carry += warp_sums[kSingleThreads / 32 - 1];
+        __syncthreads();  // warp_sums is rewritten by the next tile
+    }
+}
+
 // ---------------------------------------------------------------- radix
 
 constexpr uint32_t kRadixBits = 8;
@@ -263,8 +308,13 @@ int radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, uin
         uint32_t* kout = cur ? k0 : k1;
         uint32_t* vout = cur ? v0 : v1;
         k_radix_hist<<<ntiles, kRadixThreads, 0, stream>>>(kin, n, shift, ntiles, hist);
-        cudaError_t e = scan_u32(hist, hist, nhist, nullptr, nhist, nullptr, ScanInput::kValue, scan_tmp, stream);
-        if (e != cudaSuccess) { *err = e; return cur; }
+        if (nhist <= kSingleMax) {
+            k_scan_single<<<1, kSingleThreads, 0, stream>>>(hist, hist, nhist);
+            ++g_launches;
+        } else {
+            cudaError_t e = scan_u32(hist, hist, nhist, nullptr, nhist, nullptr, ScanInput::kValue, scan_tmp, stream);
+            if (e != cudaSuccess) { *err = e; return cur; }
+        }
         k_radix_scatter<<<ntiles, kRadixThreads, 0, stream>>>(kin, vin, kout, vout, n, shift, ntiles, hist);
         g_launches += 2;
         cur ^= 1;
