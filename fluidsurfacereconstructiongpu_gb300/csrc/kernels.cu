@@ -608,17 +608,25 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
 // Blocks of two warps: a warp without involved particles exits at once, and
 // a small block gives its registers back as soon as its two warps are done,
 // so the working warps' blocks fill the SM.
+// P lanes per particle: each takes every P-th candidate of the particle's
+// walk and the lanes' sums and counts are joined at the end (the covariance
+// sums may be taken in any order, the count is an integer).  P = 4 for
+// small frames, whose particles alone are too few warps to fill the GPU; P
+// = 1 otherwise (four lanes measured slower once the GPU is full).
 constexpr int kCovThreads = 64;
+constexpr uint32_t kCovSplitBelow = 1u << 17;  // particles below which P = 4
 #ifndef FSR_COV_MIN_BLOCKS
 #define FSR_COV_MIN_BLOCKS 16
 #endif
 
+template <int P>
 __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs a, Counters* ctr)
 {
     __shared__ float4 s_q[kCovThreads];  // 32 staged candidates per warp
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) / P;
+    const uint32_t sub = threadIdx.x % P;
     bool act = t < a.n && a.invol[a.skeys[t]];
-    warp_count(&ctr->n_involved, act);
+    warp_count(&ctr->n_involved, act && sub == 0);
     if (__all_sync(0xffffffffu, !act)) return;
     const int lane = threadIdx.x & 31;
     float4* sq = s_q + (threadIdx.x & ~31u);
@@ -703,24 +711,35 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
                 for (uint32_t base = beg; base < end; base += 32) {
                     const uint32_t cnt = stage_in_box(a.sorted, base, end, box, sq, lane);
                     __syncwarp();
-                    uint32_t k = 0;
-                    for (; k + 4 <= cnt; k += 4) {
-                        const float4 q0 = sq[k], q1 = sq[k + 1], q2 = sq[k + 2], q3 = sq[k + 3];
-                        const bool n0 = near(q0), n1 = near(q1), n2 = near(q2), n3 = near(q3);
-                        if (n0) take(q0);
-                        if (n1) take(q1);
-                        if (n2) take(q2);
-                        if (n3) take(q3);
+                    if (act) {
+                        uint32_t k = sub;
+                        for (; k + 3 * P < cnt; k += 4 * P) {
+                            const float4 q0 = sq[k], q1 = sq[k + P], q2 = sq[k + 2 * P], q3 = sq[k + 3 * P];
+                            const bool n0 = near(q0), n1 = near(q1), n2 = near(q2), n3 = near(q3);
+                            if (n0) take(q0);
+                            if (n1) take(q1);
+                            if (n2) take(q2);
+                            if (n3) take(q3);
+                        }
+                        for (; k < cnt; k += P) take(sq[k]);
+                        since += cnt / P;
+                        if (since >= 32) fold();
                     }
-                    for (; k < cnt; ++k) take(sq[k]);
-                    since += cnt;
-                    if (since >= 32) fold();
                     __syncwarp();
                 }
             }
-        if (!act) return;
-    } else {
-        if (!act) return;
+    } else if (act && P > 1) {
+        for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
+            for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
+                uint32_t beg, end;
+                row_range(w.lo[0], w.hi[0], yy, zz, beg, end);
+                for (uint32_t i = beg + sub; i < end; i += P) {
+                    const float4 q = __ldg(&a.sorted[i]);
+                    if (near(q)) take(q);
+                    if (++since >= 32) fold();
+                }
+            }
+    } else if (act) {
         for (int zz = w.lo[2]; zz <= w.hi[2]; ++zz)
             for (int yy = w.lo[1]; yy <= w.hi[1]; ++yy) {
                 uint32_t beg, end;
@@ -742,6 +761,23 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
             }
     }
     fold();
+    // join the particle's lanes (every lane of the warp takes part)
+#pragma unroll
+    for (int o = 1; o < P; o <<= 1) {
+        auto join = [&](Kahan& k) {
+            const float s = __shfl_xor_sync(0xffffffffu, k.s, o), c = __shfl_xor_sync(0xffffffffu, k.c, o);
+            k.add(s - c);
+        };
+        join(acc.tot.wsum);
+        join(acc.tot.c11);
+        join(acc.tot.c22);
+        join(acc.tot.c33);
+        join(acc.tot.c12);
+        join(acc.tot.c13);
+        join(acc.tot.c23);
+        nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    }
+    if (!act || sub != 0) return;
     const CovAccum& sums = acc.tot;
     float G[9];
     const float rmax = covariance_to_G(sums, nn, a.min_neighbors, a.h, a.h2, a.h_inv, G, &ctr->n_fp64);
@@ -1292,7 +1328,10 @@ void launch_cov(const KernelCtx& c, const CovArgs& a0, Counters* ctr)
     a.R_rcp = 1.0f / a.R;
     a.R_le2 = sqrt_threshold(a.R, true);
     a.coop_ok = (a.R + a.R * 1.0001f + 1e-4f * a.sp.cs) < 2.0f * a.sp.cs * 0.9999f ? 1 : 0;
-    k_cov<<<blocks_for(a.n, kCovThreads), kCovThreads, 0, c.stream>>>(a, ctr);
+    if (a.n < kCovSplitBelow)
+        k_cov<4><<<blocks_for((uint64_t)a.n * 4, kCovThreads), kCovThreads, 0, c.stream>>>(a, ctr);
+    else
+        k_cov<1><<<blocks_for(a.n, kCovThreads), kCovThreads, 0, c.stream>>>(a, ctr);
     ++g_launches;
 }
 
