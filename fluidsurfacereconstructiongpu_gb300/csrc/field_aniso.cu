@@ -831,9 +831,6 @@ __device__ __forceinline__ bool within(float4 q, float4 lo, float4 hi, float r2)
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r2;
 }
 
-#ifndef FSR_ISO_PAIRS
-#define FSR_ISO_PAIRS 1
-#endif
 template <bool TC01>
 __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandView band, uint32_t ratio, Counters* ctr)
 {
@@ -923,7 +920,6 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                 ay = w.sum[2][t][lane];
                                 az = w.sum[3][t][lane];
                             }
-#if FSR_ISO_PAIRS
                             // two candidates per step, their terms added in order
                             for (uint32_t mm = m; mm;) {
                                 const int ka = __ffs(mm) - 1;
@@ -958,26 +954,6 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                     }
                                 }
                             }
-#else
-                            for (uint32_t mm = m; mm; mm &= mm - 1u) {
-                                const float4 qq = w.rec[__ffs(mm) - 1];
-                                const float dx = qq.x - vp.x, dy = qq.y - vp.y, dz = qq.z - vp.z;
-                                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                                if (TC01) {
-                                    if (d2 <= a.h2) {
-                                        const float u = d2 * a.inv_h2 * 0.5f;
-                                        ws += u * u - u + 0.25f;
-                                    }
-                                } else if (d2 < a.h2) {
-                                    const float u = 1.0f - d2 * a.inv_h2;
-                                    const float wt = u * u * u;
-                                    ws += wt;
-                                    ax = fmaf(dx, wt, ax);
-                                    ay = fmaf(dy, wt, ay);
-                                    az = fmaf(dz, wt, az);
-                                }
-                            }
-#endif
                             w.sum[0][t][lane] = ws;
                             if (!TC01) {
                                 w.sum[1][t][lane] = ax;

@@ -827,9 +827,6 @@ __device__ __forceinline__ float field_at(const McArgs& a, int x, int y, int z)
     return r < a.cap_band ? __ldg(a.band.phi + r) : a.fill;  // r >= cap only in a frame that is re-run
 }
 
-#ifndef FSR_CLASSIFY_ROWS
-#define FSR_CLASSIFY_ROWS 1
-#endif
 // detectValidSurfaceCubes (cu:328-364): a band vertex as cube origin is
 // valid when all 8 corners are band vertices and the case emits triangles.
 __global__ void k_mc_classify(McArgs a, const Counters* ctr)
@@ -841,7 +838,6 @@ __global__ void k_mc_classify(McArgs a, const Counters* ctr)
         uint32_t x, y, z;
         unlin3(v, a.sc, x, y, z);
         uint32_t info = 0;
-#if FSR_CLASSIFY_ROWS
         // the cube's corners as 4 rows of two x-neighbours, (dy, dz) in
         // {0,1}^2: one bitset word (two when the pair straddles a word) and
         // one prefix per row give both memberships and both ranks (the x + 1
@@ -877,33 +873,6 @@ __global__ void k_mc_classify(McArgs a, const Counters* ctr)
                 if (in_cap) info = (uint32_t)c_mc.nverts[cs] | (cs << 8);
             }
         }
-#else
-        if (x < a.sc.res[0] - 1 && y < a.sc.res[1] - 1 && z < a.sc.res[2] - 1) {
-            bool all = true;
-            uint32_t ids[8];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                ids[i] = v + (uint32_t)mc::cornerDx(i) + (uint32_t)mc::cornerDy(i) * rx +
-                         (uint32_t)mc::cornerDz(i) * rxy;
-                all = all && band_has(a.band, ids[i]);
-            }
-            if (all) {
-                uint32_t cs = 0;
-                bool in_cap = true;
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const uint32_t r = i == 0 ? t : (i == 4 ? t + 1 : band_rank(a.band, ids[i]));
-                    // ranks beyond the capacity only occur in a frame that overflowed and is re-run
-                    if (r >= a.cap_band) {
-                        in_cap = false;
-                        break;
-                    }
-                    if (__ldg(a.band.phi + r) <= a.iso) cs |= 1u << i;
-                }
-                if (in_cap) info = (uint32_t)c_mc.nverts[cs] | (cs << 8);
-            }
-        }
-#endif
         a.mc[t] = info;
     }
 }
