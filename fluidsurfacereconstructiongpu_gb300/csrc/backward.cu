@@ -418,9 +418,9 @@ __device__ void g_to_c(const T V[3][3], const T l[3], float h_inv, const float g
 // sq at a time (one load per particle for the whole warp); the caller sets
 // coop only when every particle the union adds fails each lane's own range
 // test, so each lane still sees exactly the particles that matter to it.
-// Staged particles outside the box of the active lanes' centres (cx, cy, cz)
-// grown by r are dropped (they fail every lane's range test); the others
-// keep their order, their index rides in the staged w.
+// Staged particles beyond r of the box of the active lanes' centres (cx,
+// cy, cz) are dropped (they fail every lane's range test); the others keep
+// their order, their index rides in the staged w.
 template <class Fn>
 __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool coop, const Grid& sp,
                                              const uint2* __restrict__ ranges, const float4* __restrict__ sorted,
@@ -458,7 +458,7 @@ __device__ __forceinline__ void walk_windows(const Window& w, bool active, bool 
                     bool keep = false;
                     if (b + lane < end) {
                         q = __ldg(&sorted[b + lane]);
-                        keep = box.holds(q);
+                        keep = box.keeps(q);
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, keep);
                     if (keep) sq[__popc(m & ((1u << lane) - 1u))] = make_float4(q.x, q.y, q.z, __uint_as_float(b + lane));

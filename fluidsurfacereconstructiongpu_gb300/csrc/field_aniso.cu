@@ -201,10 +201,13 @@ constexpr int kFWarps = kFT / 32;
 constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept in registers)
 constexpr int kPassVerts = 32 * kPassTiles;
 constexpr int kMoments = 35;             // moments of the unscaled kernel's polynomial (unscaled_sum)
+constexpr int kPairF4 = 5;               // float4 per pair block of listed candidates (list_pair_record)
 
 // Per-warp shared memory of the forward kernel.
 struct WarpSlice {
-    float4 rec[32 * 3];          // the current chunk's candidate records, one per lane
+    float4 rec[80];              // the current chunk's candidates: 5 float2 per lane (involved, stage_record),
+                                 // a float4 per lane (the others)
+    float4 lst[16 * kPairF4];    // one tile's involved candidates in lane order, two to a pair block
     uint32_t vloc[kPassVerts];   // the pass's band vertices: index in the group's box (vert_loc)
     uint32_t vrank[kPassVerts];  // and band rank
     float4 box[2 * kPassTiles];  // per tile: lo, hi
@@ -324,21 +327,62 @@ __device__ uint32_t warp_candidates(const Grid& sp, const uint2* __restrict__ ra
     return running;
 }
 
-// (1 - q2)^3 and the coefficient of the record at r for vertex v; false
-// when v lies outside the support (q2 >= 1: the term is exactly zero).
-__device__ __forceinline__ bool term(const float4* r, float4 v, float& u3, float& coef)
+// A staged involved candidate: 10 floats per lane, as 5 float2
+//   (x~, y~) (z~, M00) (2M01, 2M02) (M11, 2M12) (M22, coef)
+// (M = G^T G; coef = sigma det(G) m / rho).
+__device__ __forceinline__ void stage_record(float2* rec, int lane, float4 r0, float4 m0, float4 m1)
 {
-    // r[0] = (x~, r2max), r[1] = (M00, 2 M01, 2 M02, coef), r[2] = (M11, 2 M12, M22, 0)
-    // with M = G^T G, so q2 = |G d|^2 = d^T M d for d = x~ - v
-    const float4 q0 = r[0], m0 = r[1], m1 = r[2];
-    const float dx = q0.x - v.x, dy = q0.y - v.y, dz = q0.z - v.z;
-    const float t1 = fmaf(m0.x, dx, fmaf(m0.y, dy, m0.z * dz));
-    const float t2 = fmaf(m1.x, dy, m1.y * dz);
-    const float q2 = fmaf(dx, t1, fmaf(dy, t2, dz * (m1.z * dz)));
-    const float u = 1.0f - q2;
-    u3 = u * u * u;
-    coef = m0.w;
-    return q2 < 1.0f;
+    float2* d = rec + 5 * lane;
+    d[0] = make_float2(r0.x, r0.y);
+    d[1] = make_float2(r0.z, m0.x);
+    d[2] = make_float2(m0.y, m0.z);
+    d[3] = make_float2(m1.x, m1.y);
+    d[4] = make_float2(m1.z, m0.w);
+}
+
+// A tile's candidates are listed two to a pair block of 5 float4: entry pos
+// of the list in the x (and z) components, entry pos + 1 in y (and w), so
+// that each float2 of the block holds one quantity of both candidates and
+// feeds one packed FP32x2 operation:
+//   (x~, x~') (y~, y~') | (z~, z~') (M00, M00') | (2M01, 2M01') (2M02, 2M02') |
+//   (M11, M11') (2M12, 2M12') | (M22, M22') (coef, coef')
+__device__ __forceinline__ void list_pair_record(const float2* rec, int lane, float* lst, uint32_t pos)
+{
+    const float2* src = rec + 5 * lane;
+    float* d = lst + (pos >> 1) * (4 * kPairF4) + (pos & 1u);
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+        const float2 v = src[c];
+        d[4 * c] = v.x;
+        d[4 * c + 2] = v.y;
+    }
+}
+
+// The (1 - q2)^3 terms of both candidates of a pair block for vertex v
+// (nv = (-v, -v) per axis), with the operations and roundings of term()
+// applied to each component: q2 = d^T M d for d = x~ - v.
+__device__ __forceinline__ void pair_terms(const float4* P, float2 nvx, float2 nvy, float2 nvz, float2& q2,
+                                           float2& u3, float2& coef)
+{
+    const float4 A = P[0], B = P[1], C = P[2], D = P[3], E = P[4];
+    const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nvx);
+    const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nvy);
+    const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nvz);
+    float2 t1 = __fmul2_rn(make_float2(C.z, C.w), dz);
+    t1 = __ffma2_rn(make_float2(C.x, C.y), dy, t1);
+    t1 = __ffma2_rn(make_float2(B.z, B.w), dx, t1);
+    float2 t2 = __fmul2_rn(make_float2(D.z, D.w), dz);
+    t2 = __ffma2_rn(make_float2(D.x, D.y), dy, t2);
+    float2 q = __fmul2_rn(make_float2(E.x, E.y), dz);
+    q = __fmul2_rn(dz, q);
+    q = __ffma2_rn(dy, t2, q);
+    q = __ffma2_rn(dx, t1, q);
+    // 1 - q2 as fma(q2, -1, 1): the product is exact, so one rounding, as in
+    // the subtraction
+    const float2 u = __ffma2_rn(q, make_float2(-1.0f, -1.0f), make_float2(1.0f, 1.0f));
+    u3 = __fmul2_rn(__fmul2_rn(u, u), u);
+    q2 = q;
+    coef = make_float2(E.z, E.w);
 }
 
 __device__ __forceinline__ bool reaches(float4 r0, float4 lo, float4 hi)
@@ -680,12 +724,7 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
                     r0 = __ldg(qsrc);
                     const float4 r1 = __ldg(qsrc + 1), r2 = __ldg(qsrc + 2);
                     keep = reaches(r0, pl, ph);
-                    if (keep) {
-                        float4* dst = w.rec + 3 * lane;
-                        dst[0] = r0;
-                        dst[1] = r1;
-                        dst[2] = r2;
-                    }
+                    if (keep) stage_record(reinterpret_cast<float2*>(w.rec), lane, r0, r1, r2);
                 }
                 const uint32_t any = __ballot_sync(0xffffffffu, keep);
                 __syncwarp();
@@ -694,35 +733,47 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
                     for (int t = 0; t < kPassTiles; ++t) {
                         if ((uint32_t)t < ntiles) {
                             const uint32_t m = __ballot_sync(0xffffffffu, keep && reaches(r0, w.box[2 * t], w.box[2 * t + 1]));
-                            const uint32_t v = 32 * t + lane;
-                            if (m && v < nv) {
-                                const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
-                                // the chunk's terms are summed on their own and
-                                // then added to the vertex's sum with the
-                                // rounding error of that addition (two-sum)
-                                // kept in the second sum: with tens of
-                                // thousands of neighbours one running FP32 sum
-                                // drifts by more than 1e-5 of the field
-                                float s = 0.f;
-                                // two kept candidates per step, evaluated without
-                                // branches; their terms enter the sum in order
-                                for (uint32_t mm = m; mm;) {
-                                    const int ka = __ffs(mm) - 1;
-                                    mm &= mm - 1u;
-                                    const bool two = mm != 0u;
-                                    const int kb = two ? __ffs(mm) - 1 : ka;
-                                    mm &= two ? mm - 1u : ~0u;
-                                    float ua, ub, ca, cb;
-                                    const bool ina = term(w.rec + 3 * ka, vp, ua, ca);
-                                    const bool inb = term(w.rec + 3 * kb, vp, ub, cb);
-                                    if (ina) s = fmaf(ca, ua, s);
-                                    if (two && inb) s = fmaf(cb, ub, s);
+                            if (m) {
+                                // the candidates that reach the tile, listed in
+                                // lane order two to a pair block
+                                if ((m >> lane) & 1u)
+                                    list_pair_record(reinterpret_cast<const float2*>(w.rec), lane,
+                                                     reinterpret_cast<float*>(w.lst), __popc(m & ((1u << lane) - 1u)));
+                                __syncwarp();
+                                const uint32_t v = 32 * t + lane;
+                                if (v < nv) {
+                                    const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
+                                    // the chunk's terms are summed on their own and
+                                    // then added to the vertex's sum with the
+                                    // rounding error of that addition (two-sum)
+                                    // kept in the second sum: with tens of
+                                    // thousands of neighbours one running FP32 sum
+                                    // drifts by more than 1e-5 of the field
+                                    float s = 0.f;
+                                    // one pair block per step, both candidates
+                                    // evaluated at once by packed operations; the
+                                    // terms of vertices inside the support enter
+                                    // the sum in list (lane) order
+                                    const float2 nvx = make_float2(-vp.x, -vp.x), nvy = make_float2(-vp.y, -vp.y),
+                                                 nvz = make_float2(-vp.z, -vp.z);
+                                    const uint32_t cnt = __popc(m);
+                                    // not unrolled: copies of the body crowd the
+                                    // instruction cache (measured: fetch stalls
+                                    // doubled and the 2^18-particle frame slowed)
+#pragma unroll 1
+                                    for (uint32_t j = 0; j < cnt; j += 2) {
+                                        float2 q2, u3, c;
+                                        pair_terms(w.lst + (j >> 1) * kPairF4, nvx, nvy, nvz, q2, u3, c);
+                                        if (q2.x < 1.0f) s = fmaf(c.x, u3.x, s);
+                                        if (j + 1 < cnt && q2.y < 1.0f) s = fmaf(c.y, u3.y, s);
+                                    }
+                                    const float a0 = w.psum[t][lane];
+                                    const float t0 = a0 + s;
+                                    const float bp = t0 - a0;
+                                    w.psum[t][lane] = t0;
+                                    w.usum[t][lane] += (a0 - (t0 - bp)) + (s - bp);
                                 }
-                                const float a0 = w.psum[t][lane];
-                                const float t0 = a0 + s;
-                                const float bp = t0 - a0;
-                                w.psum[t][lane] = t0;
-                                w.usum[t][lane] += (a0 - (t0 - bp)) + (s - bp);
+                                __syncwarp();
                             }
                         }
                     }

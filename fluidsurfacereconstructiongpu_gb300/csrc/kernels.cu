@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) k_colorfield(const float4* __restric
                     bool keep = false;
                     if (b + lane < end) {
                         q = __ldg(&sorted[b + lane]);
-                        keep = box.holds(q);
+                        keep = box.keeps(q);
                     }
                     const uint32_t mk = __ballot_sync(0xffffffffu, keep);
                     if (keep) {
@@ -440,17 +440,22 @@ __global__ void k_band_list(const uint32_t* __restrict__ bits, const uint32_t* _
 }
 
 
-// Stages the warp's next chunk of candidates [base, end): the ones inside
-// the box go to sq in their order; returns how many.
+// Stages the warp's next chunk of candidates [base, end): the ones within
+// the box's reach go to sq in their order; returns how many.  nbox is the
+// number inside the grown box itself, which the callers count towards their
+// chunk sums exactly as before the reach test was added, so that the sums
+// join their totals at the same points.
 __device__ __forceinline__ uint32_t stage_in_box(const float4* __restrict__ src, uint32_t base, uint32_t end,
-                                                 const WarpBox& box, float4* sq, int lane)
+                                                 const WarpBox& box, float4* sq, int lane, uint32_t& nbox)
 {
     float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool keep = false;
+    bool in = false, keep = false;
     if (base + lane < end) {
         q = __ldg(&src[base + lane]);
-        keep = box.holds(q);
+        in = box.holds(q);
+        keep = in && box.reaches(q);
     }
+    nbox = __popc(__ballot_sync(0xffffffffu, in));
     const uint32_t m = __ballot_sync(0xffffffffu, keep);
     if (keep) sq[__popc(m & ((1u << lane) - 1u))] = q;
     return __popc(m);
@@ -559,10 +564,11 @@ __global__ void __launch_bounds__(kThreads, FSR_SMOOTH_MIN_BLOCKS) k_smooth(cons
                 uint32_t beg, end;
                 row_range(ulo[0], uhi[0], yy, zz, beg, end);
                 for (uint32_t base = beg; base < end; base += 32) {
-                    const uint32_t cnt = stage_in_box(sorted, base, end, box, sq, lane);
+                    uint32_t nbox;
+                    const uint32_t cnt = stage_in_box(sorted, base, end, box, sq, lane, nbox);
                     __syncwarp();
                     for (uint32_t k = 0; k < cnt; ++k) add(sq[k]);
-                    since += cnt;
+                    since += nbox;
                     if (since >= 32) fold();
                     __syncwarp();
                 }
@@ -709,7 +715,8 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
                 uint32_t beg, end;
                 row_range(ulo[0], uhi[0], yy, zz, beg, end);
                 for (uint32_t base = beg; base < end; base += 32) {
-                    const uint32_t cnt = stage_in_box(a.sorted, base, end, box, sq, lane);
+                    uint32_t nbox;
+                    const uint32_t cnt = stage_in_box(a.sorted, base, end, box, sq, lane, nbox);
                     __syncwarp();
                     if (act) {
                         uint32_t k = sub;
@@ -722,7 +729,7 @@ __global__ void __launch_bounds__(kCovThreads, FSR_COV_MIN_BLOCKS) k_cov(CovArgs
                             if (n3) take(q3);
                         }
                         for (; k < cnt; k += P) take(sq[k]);
-                        since += cnt / P;
+                        since += nbox / P;
                         if (since >= 32) fold();
                     }
                     __syncwarp();
