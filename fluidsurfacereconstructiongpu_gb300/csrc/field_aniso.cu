@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kFT, FSR_FIELD_MIN_BLOCKS) k_field_aniso_group
 // particles in sorted order); candidates of the window cells the per-vertex
 // walk narrows away lie beyond h and add nothing.
 struct IsoSlice {
-    float4 rec[32];                // the current chunk's candidates, one per lane
+    float4 lst[32];                // one tile's candidates in lane order, two to a pair block (list_iso_pair)
     uint32_t vloc[kPassVerts];     // the pass's band vertices: index in the group's box (vert_loc)
     uint32_t vrank[kPassVerts];    // and band rank
     float4 box[2 * kPassTiles];    // per tile: lo, hi
@@ -880,6 +880,19 @@ __device__ __forceinline__ bool within(float4 q, float4 lo, float4 hi, float r2)
     const float gy = fmaxf(0.f, fmaxf(lo.y - q.y, q.y - hi.y));
     const float gz = fmaxf(0.f, fmaxf(lo.z - q.z, q.z - hi.z));
     return fmaf(gx, gx, fmaf(gy, gy, gz * gz)) < r2;
+}
+
+// A tile's candidates listed two to a pair block of 2 float4: entry pos in
+// the x and z components, entry pos + 1 in y and w,
+//   (x, x') (y, y') | (z, z') (unused)
+// so that the offsets and squared distances of both are formed by packed
+// FP32x2 operations.
+__device__ __forceinline__ void list_iso_pair(float4 q, float* lst, uint32_t pos)
+{
+    float* d = lst + (pos >> 1) * 8 + (pos & 1u);
+    d[0] = q.x;
+    d[2] = q.y;
+    d[4] = q.z;
 }
 
 template <bool TC01>
@@ -952,7 +965,6 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                     while (r < 8 && w.rp[r + 1] <= j) ++r;
                     q = __ldg(&a.sorted[w.rb[r] + (j - w.rp[r])]);
                     keep = within(q, pl, ph, cr2);
-                    if (keep) w.rec[lane] = q;
                 }
                 const uint32_t any = __ballot_sync(0xffffffffu, keep);
                 __syncwarp();
@@ -961,8 +973,14 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                     for (int t = 0; t < kPassTiles; ++t) {
                         if ((uint32_t)t >= ntiles) break;
                         const uint32_t m = __ballot_sync(0xffffffffu, keep && within(q, w.box[2 * t], w.box[2 * t + 1], cr2));
+                        if (!m) continue;
+                        // the candidates within h of the tile, listed in lane
+                        // order two to a pair block
+                        if ((m >> lane) & 1u)
+                            list_iso_pair(q, reinterpret_cast<float*>(w.lst), __popc(m & ((1u << lane) - 1u)));
+                        __syncwarp();
                         const uint32_t v = 32 * t + lane;
-                        if (m && v < nv) {
+                        if (v < nv) {
                             const float4 vp = vert_pos(w.vloc[w.order[v]], lo, a.sc);
                             float ws = w.sum[0][t][lane];
                             float ax = 0.f, ay = 0.f, az = 0.f;
@@ -971,18 +989,25 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                 ay = w.sum[2][t][lane];
                                 az = w.sum[3][t][lane];
                             }
-                            // two candidates per step, their terms added in order
-                            for (uint32_t mm = m; mm;) {
-                                const int ka = __ffs(mm) - 1;
-                                mm &= mm - 1u;
-                                const bool two = mm != 0u;
-                                const int kb = two ? __ffs(mm) - 1 : ka;
-                                mm &= two ? mm - 1u : ~0u;
-                                const float4 qa = w.rec[ka], qb = w.rec[kb];
-                                const float dxa = qa.x - vp.x, dya = qa.y - vp.y, dza = qa.z - vp.z;
-                                const float dxb = qb.x - vp.x, dyb = qb.y - vp.y, dzb = qb.z - vp.z;
-                                const float d2a = fmaf(dxa, dxa, fmaf(dya, dya, dza * dza));
-                                const float d2b = fmaf(dxb, dxb, fmaf(dyb, dyb, dzb * dzb));
+                            const float2 nvx = make_float2(-vp.x, -vp.x), nvy = make_float2(-vp.y, -vp.y),
+                                         nvz = make_float2(-vp.z, -vp.z);
+                            const uint32_t cnt = __popc(m);
+                            // one pair block per step: offsets and squared
+                            // distances of both by packed operations (the
+                            // roundings of the scalar forms), the rest per
+                            // candidate; terms added in list (lane) order.  Not
+                            // unrolled: copies of the body crowd the
+                            // instruction cache
+#pragma unroll 1
+                            for (uint32_t j = 0; j < cnt; j += 2) {
+                                const bool two = j + 1 < cnt;
+                                const float4 A = w.lst[j], B = w.lst[j + 1];  // pair block j / 2
+                                const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nvx);
+                                const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nvy);
+                                const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nvz);
+                                const float2 d2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                                const float dxa = dx.x, dya = dy.x, dza = dz.x, d2a = d2.x;
+                                const float dxb = dx.y, dyb = dy.y, dzb = dz.y, d2b = d2.y;
                                 if (TC01) {
                                     const float ua = d2a * a.inv_h2 * 0.5f, ub = d2b * a.inv_h2 * 0.5f;
                                     const float ta = ua * ua - ua + 0.25f, tb = ub * ub - ub + 0.25f;
@@ -1012,6 +1037,7 @@ __global__ void __launch_bounds__(kFT) k_field_iso_grouped(IsoFieldArgs a, BandV
                                 w.sum[3][t][lane] = az;
                             }
                         }
+                        __syncwarp();  // the list is rewritten for the next tile
                     }
                 }
                 __syncwarp();
