@@ -359,8 +359,11 @@ __device__ __forceinline__ void list_pair_record(const float2* rec, int lane, fl
 }
 
 // The (1 - q2)^3 terms of both candidates of a pair block for vertex v
-// (nv = (-v, -v) per axis), with the operations and roundings of term()
-// applied to each component: q2 = d^T M d for d = x~ - v.
+// (nv = (-v, -v) per axis): q2 = d^T M d for d = x~ - v, each component
+// rounded as the scalar form
+//   t1 = fma(M00, dx, fma(2M01, dy, 2M02 dz)),  t2 = fma(M11, dy, 2M12 dz),
+//   q2 = fma(dx, t1, fma(dy, t2, dz (M22 dz))),  (1 - q2)^3 = ((1 - q2)^2)(1 - q2)
+// (no product feeds a separate sum, so no contraction can change a rounding).
 __device__ __forceinline__ void pair_terms(const float4* P, float2 nvx, float2 nvy, float2 nvz, float2& q2,
                                            float2& u3, float2& coef)
 {
