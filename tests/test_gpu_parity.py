@@ -130,3 +130,61 @@ def test_zb05_plain_small_workload_baseline_iso():
     fr = synthetic.lattice_cube(32, 0.0125, seed=1)
     rep = _run("zb05", fr, grid_ratio=8, iso=0.5)
     assert rep["triangles"] == 0
+
+
+
+def _translated(fr, offset):
+    o = np.float32(offset)
+    fr.pos = (fr.pos + o).astype(np.float32)
+    fr.bbox_min = (fr.bbox_min + o).astype(np.float32)
+    fr.bbox_max = (fr.bbox_max + o).astype(np.float32)
+    return fr
+
+
+def _run_exact(method, fr, **kw):
+    """One frame against the FP32 oracle on the stages that are bit-exact by
+    construction: sort order, cell ranges, sorted positions, surface flags,
+    involved counts and FP32 means (Yu13), band vertices.  (The FP64 checks of
+    compare_frame use absolute tolerances scaled for coordinates of order 1.)
+    Returns the number of band vertices."""
+    import torch
+    from fluidsurfacereconstructiongpu_gb300 import api
+    from oracle import pipeline as P
+
+    params = P.FrameParams(method=method, h=fr.h, particle_radius=fr.particle_radius, mass=fr.mass,
+                           iso=kw.get("iso"), ratio=kw.get("grid_ratio"), cell_scale=kw.get("cell_size_scale"),
+                           lam=kw.get("smoothing_lambda", 0.5),
+                           aniso_radius=(kw["aniso_radius_over_h"] * fr.h if "aniso_radius_over_h" in kw else None))
+    rec = api.Reconstructor(method, 0, keep_intermediates=True, **kw)
+    rec.reconstruct(torch.from_numpy(np.ascontiguousarray(fr.pos)).cuda(),
+                    torch.from_numpy(np.ascontiguousarray(fr.density)).cuda(), api.header_of(fr))
+    o32 = P.run_frame("oracle32", fr.pos, fr.density, fr.bbox_min, fr.bbox_max, params)
+    assert np.array_equal(rec.debug("perm"), o32.perm), "stable sort order differs"
+    assert np.array_equal(rec.debug("ranges"), o32.ranges), "cell ranges differ"
+    assert np.array_equal(rec.debug("sorted_xyz"), o32.pos), "sorted positions differ"
+    assert np.array_equal(rec.debug("surface_flags"), o32.sflag), "surface particle flags differ"
+    if method == "yu13":
+        assert np.array_equal(rec.debug("involved_counts"), o32.ninv), "involved counts differ"
+        assert np.array_equal(rec.debug("mean"), o32.mean32), "weighted means differ"
+    sv = rec.debug("band")
+    assert np.array_equal(sv, o32.sv), "band vertices differ"
+    rec.close()
+    return int(sv.size)
+
+
+def test_yu13_frame_away_from_the_origin():
+    """The dam-break settings of test_yu13_dam_break_workload_parameters with
+    the frame moved by +10 on each axis (about 170 cells from the origin):
+    the warp culls of the smoothing and covariance kernels, whose margins
+    grow with the coordinates' magnitude, still keep every neighbour, so the
+    FP32 means, counts and band equal the oracle's bit for bit."""
+    from fluidsurfacereconstructiongpu_gb300 import synthetic
+    fr = _translated(synthetic.dam_break(n_total=20000, r=0.012, seed=5), 10.0)
+    nb = _run_exact("yu13", fr, smoothing_lambda=0.9, aniso_radius_over_h=1.0, cell_size_scale=1.25, grid_ratio=10)
+    assert nb > 0
+
+
+def test_akinci_frame_away_from_the_origin():
+    """A lattice moved by +10 on each axis through the colour field's warp
+    culls: surface flags and band bit for bit."""
+    assert _run_exact("akinci", _translated(_lattice(12), 10.0)) > 0
