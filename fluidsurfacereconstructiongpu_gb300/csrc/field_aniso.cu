@@ -5,19 +5,24 @@
 // around the spatial cell its FP32 position falls in; every vertex that
 // falls in the same cell has the same window.  Along each axis that cell
 // index is a non-decreasing function of the vertex index, so the vertices
-// of one cell form an index box, found exactly without sorting.  One block
-// handles one such group:
-//   1. it lists the group's band vertices (bitset tests, order kept per
-//      warp) and their rank in the band;
+// of one cell form an index box, found exactly without sorting.  One warp
+// handles one such group (or one z slab of it, for frames with few groups),
+// taken from a work counter:
+//   1. it lists the group's band vertices row by row from the bitset, with
+//      their rank in the band, in passes of up to 256 vertices ordered into
+//      eight brick tiles of 32;
 //   2. it lists the window's candidate cells, dropping involved cells that
 //      lie beyond the reach (largest support radius + smoothing shift) of all
 //      their particles from the group's vertex box;
-//   3. it streams the candidates through shared memory in chunks of 256
-//      records; each warp keeps the candidates whose support can reach the
-//      bounding box of its own vertices, and each lane evaluates only those.
+//   3. it streams the involved candidates 32 at a time (one record per lane,
+//      kept in shared memory when its support reaches the pass's box); per
+//      tile, the candidates that reach the tile are listed two to a pair
+//      block and each lane evaluates one block per step for its vertex with
+//      packed FP32x2 operations.
 // Particles of non-involved cells use the unscaled kernel (cuh:312-322),
-// written here as G = I with support 1, so one evaluation path serves both.
-// Only terms that are exactly zero are skipped; the summation order is the
+// G = I with support 1: their part of each vertex's sum is the group's
+// moment polynomial where it applies, else they are streamed as well.  Only
+// terms that are exactly zero are skipped; the summation order is the
 // candidate order, the same for every vertex, so results are deterministic.
 #include "kernels.h"
 #include "backward.h"
