@@ -203,7 +203,7 @@ constexpr int kFT = 128;                 // threads per block of the forward ker
 #define FSR_FIELD_MIN_BLOCKS 6               // blocks per SM of the anisotropic field (80 registers)
 #endif
 constexpr int kFWarps = kFT / 32;
-constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept in registers)
+constexpr int kPassTiles = 8;            // 32-vertex tiles per pass (sums kept per lane in the warp's slice)
 constexpr int kPassVerts = 32 * kPassTiles;
 constexpr int kMoments = 35;             // moments of the unscaled kernel's polynomial (unscaled_sum)
 constexpr int kPairF4 = 5;               // float4 per pair block of listed candidates (list_pair_record)
